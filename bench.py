@@ -1,0 +1,362 @@
+"""Benchmark: ParaGraph GPU build path (K0..K11) on GB300.
+
+Workload (the 1M x 200 inner-product configuration): N = Q = 1,000,000 base points, D = 200,
+float32, mixture of 64 Gaussians; training queries from the shifted/rotated recipe; exact float32
+inner-product top-128 ground truth; out-degree M = 32, beam L = 64.  Inputs are seeded synthetic
+stand-ins for the reference's datasets, generated on the GPU before timing.
+
+A step is one full build (projection + two link rounds).  `value` is distance evaluations per
+second with inputs resident in HBM (evaluations counted as the reference's distance_between /
+search distance calls; the kernels count them and the tests check the count against the oracle).
+`e2e` is the same metric through pg_build_host with pinned host buffers: base + gt host->device
+and graph + projection device->host inside the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n N] [--d D]
+
+--impl reference times the CPU restatement of the path (the oracle; the reference's own code for
+this path is GPU-only and its CPU RoarGraph path does not build on this Arm host) on all host
+cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "distance_evals_per_s (build, 1Mx200 IP, M=32, L=64)"
+UNIT = "evals/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--d", type=int, default=200)
+    ap.add_argument("--degree", type=int, default=32)
+    ap.add_argument("--beam", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="target length of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}",
+                                      f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for name, v in zip(names, s[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+def dist_init(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.impl == "ours":
+        torch.cuda.set_device(local)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def gpu_workload(args, device):
+    from paragraph_gb300 import datagen
+    base, gt = datagen.make_dataset_cuda(args.n, args.d, gt_k=128, seed=args.seed, device=device)
+    return base, gt
+
+
+def search_roofline(st, args, peak_gbs, peak_kind, rounds):
+    """Dominant kernel = the beam search (K4/K8).  Algorithmic bytes per launch: every counted
+    evaluation gathers one 4*D-byte row plus its 4-byte id, every iteration reads Kp*Kd graph ids,
+    and the launch writes n*L ids and reads each query row once."""
+    L = args.beam
+    tot_bytes = 0.0
+    tot_ms = 0.0
+    for r in range(rounds):
+        ev = st.evals_search[r]
+        it = st.search_iters[r]
+        tot_bytes += ev * (4 * args.d + 4) + it * 32 * 4 + args.n * (L * 4 + 4 * args.d)
+        tot_ms += st.ms_search[r]
+    achieved = tot_bytes / (tot_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "search_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                traffic = json.load(f).get("bytes_per_launch_1m")
+        except Exception:
+            traffic = None
+    return {"kernel": "k_search (K4/K8 beam search)", "bound": "hbm",
+            "achieved": round(achieved, 1), "peak": peak_gbs, "peak_kind": peak_kind,
+            "unit": "GB/s", "frac": round(achieved / peak_gbs, 4),
+            "traffic": traffic, "algorithmic_bytes_per_launch": round(tot_bytes / rounds)}
+
+
+def cpu_baseline_sample(args, base_np, gt_np, seconds):
+    """The oracle (CPU restatement, all host threads) on a bounded sample of the workload:
+    phase 1 (K0..K3) over all N points, then the round-1 search for as many queries as fit
+    in `seconds`.  Returns (evals/s, description, threads)."""
+    import oracle
+    import numpy as np
+    t0 = time.perf_counter()
+    proj_res = oracle.build_graph(base_np, gt_np, degree=args.degree, beam=args.beam,
+                                  link_rounds=0)
+    t1 = time.perf_counter()
+    ev = proj_res["stats"]["evals_proj_prune"] + proj_res["stats"]["evals_proj_merge"]
+    proj = proj_res["proj"]
+    km = args.beam - 32
+    qn = 2000
+    _, sev, _, _ = oracle.search(base_np, proj, km=km, q_begin=0, q_end=qn)
+    t2 = time.perf_counter()
+    per_q = (t2 - t1) / qn
+    left = max(seconds - (t2 - t0), 0.0)
+    q_more = int(min(args.n - qn, left / max(per_q, 1e-9)))
+    sev2 = 0
+    if q_more > 0:
+        _, sev2, _, _ = oracle.search(base_np, proj, km=km, q_begin=qn, q_end=qn + q_more)
+    t3 = time.perf_counter()
+    total_ev = ev + sev + sev2
+    desc = (f"oracle phase 1 (K0-K3) over all {args.n} points + round-1 search for "
+            f"{qn + q_more} queries; {total_ev} evals in {t3 - t0:.1f} s")
+    return total_ev / (t3 - t0), desc, oracle.num_threads()
+
+
+def run_reference(args):
+    """--impl reference: CPU restatement on the host cores (rank 0 only)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import numpy as np
+    import torch
+    if torch.cuda.is_available():
+        base, gt = gpu_workload(args, "cuda")
+        base_np = base.cpu().numpy()
+        gt_np = gt.cpu().numpy().view(np.uint32)
+        del base, gt
+        torch.cuda.empty_cache()
+    else:
+        from paragraph_gb300 import datagen
+        base_np, gt_np = datagen.make_dataset(args.n, args.d, seed=args.seed)
+    vals = []
+    desc = ""
+    threads = 1
+    steps = max(args.steps, 1)
+    per_step = max(min(args.cpu_seconds, 120.0 / (steps + args.warmup)), 3.0)
+    for i in range(args.warmup + steps):
+        v, desc, threads = cpu_baseline_sample(args, base_np, gt_np, per_step)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.mean(vals)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded mixture-of-Gaussians stand-in for T2I-style data)",
+            "config": {"workload": f"ParaGraph build {args.n}x{args.d} IP, gt top-128, "
+                                   f"M={args.degree}, L={args.beam}",
+                       "n": args.n, "d": args.d, "degree": args.degree, "beam": args.beam},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference's path is GPU-only; its CPU RoarGraph code is x86 AVX-512 and "
+                    "its sources are not on this host, so the CPU restatement (oracle) stands in"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    world, rank, local = dist_init(args)
+    import paragraph_gb300 as pg
+    dev = torch.device("cuda", local)
+    base, gt = gpu_workload(args, dev)
+    torch.cuda.synchronize()
+    params = pg.default_params(args.degree, args.beam)
+    n, d = base.shape
+    graph = torch.empty((n, args.degree), dtype=torch.int32, device=dev)
+    proj = torch.empty((n, 16), dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(dev)
+    h = pg.Handle(local, stream=stream)
+    launches_per_build = 8 + 8 * params.link_rounds
+    stats = []
+    for _ in range(args.warmup):
+        h.build_device(base, gt, graph, proj, params)
+    torch.cuda.synchronize()
+    barrier(world)
+    peak, peak_kind = peaks()
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        barrier(world)
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(args.steps):
+            stats.append(h.build_device(base, gt, graph, proj, params))
+        stop.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    ms_total = start.elapsed_time(stop)
+    ms_total = allmax(ms_total, world)
+    evals = stats[-1].evals_total
+    assert all(s.evals_total == evals for s in stats), "evaluation count changed between builds"
+    value = evals * args.steps * world / (ms_total / 1e3)
+    ms_step = ms_total / args.steps
+
+    e2e = None
+    if not args.no_e2e:
+        base_h = base.cpu().pin_memory()
+        gt_h = gt.cpu().pin_memory()
+        graph_h = torch.empty((n, args.degree), dtype=torch.int32).pin_memory()
+        proj_h = torch.empty((n, 16), dtype=torch.int32).pin_memory()
+        del base, gt
+        torch.cuda.empty_cache()
+        for _ in range(1):
+            h.build_host_ptr(base_h.data_ptr(), n, d, gt_h.data_ptr(), gt_h.shape[0],
+                             graph_h.data_ptr(), proj_h.data_ptr(), params)
+        barrier(world)
+        times = []
+        est = None
+        for _ in range(max(1, min(args.steps, 3))):
+            t0 = time.perf_counter()
+            est = h.build_host_ptr(base_h.data_ptr(), n, d, gt_h.data_ptr(), gt_h.shape[0],
+                                   graph_h.data_ptr(), proj_h.data_ptr(), params)
+            times.append(time.perf_counter() - t0)
+        t = allmax(statistics.mean(times), world)
+        e2e = {"value": est.evals_total * world / t, "unit": UNIT,
+               "h2d_bytes_per_step": int(est.h2d_bytes), "d2h_bytes_per_step": int(est.d2h_bytes),
+               "ms_per_step": round(t * 1e3, 2), "ms_h2d": round(est.ms_h2d, 2),
+               "ms_d2h": round(est.ms_d2h, 2)}
+        base_np = base_h.numpy()
+        gt_np = gt_h.numpy().view(np.uint32)
+    else:
+        base_np = base.cpu().numpy()
+        gt_np = gt.cpu().numpy().view(np.uint32)
+
+    roof = search_roofline(stats[-1], args, peak, peak_kind, params.link_rounds)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, desc, threads = cpu_baseline_sample(args, base_np, gt_np, args.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
+    s = stats[-1]
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32",
+                "data": "synthetic (seeded mixture-of-Gaussians stand-in for T2I-style data)",
+                "config": {"workload": f"ParaGraph build {args.n}x{args.d} IP, gt top-128, "
+                                       f"M={args.degree}, L={args.beam}",
+                           "n": args.n, "d": args.d, "q": args.n, "degree": args.degree,
+                           "beam": args.beam, "parallelism": "replicas" if world > 1 else "single",
+                           "l2": "inputs larger than L2 (base 800 MB, gt 512 MB)",
+                           "build_s": round(ms_step / 1e3, 4)},
+                "evals_per_build": evals,
+                "stage_ms": {"proj": round(s.ms_proj, 2),
+                             "search": [round(x, 2) for x in list(s.ms_search)[:params.link_rounds]],
+                             "prune": [round(x, 2) for x in list(s.ms_prune)[:params.link_rounds]],
+                             "merge": [round(x, 2) for x in list(s.ms_merge)[:params.link_rounds]]},
+                "gpu_launches": launches_per_build * args.steps,
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+    h.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,169 @@
+/*
+ * paragraph_gb300.h -- C ABI of the GB300 (sm_103a) ParaGraph graph-index builder.
+ *
+ * Drop-in for the GPU build path of ParaGraph (9p6p/ParaGraph): the twelve kernel launches
+ * K0..K11 of tests/test_t2iend.cu:974-1139 that turn base vectors plus each training query's
+ * top-128 ground-truth ids into a RoarGraph-style proximity graph.  The reference exposes that
+ * path only as kernel templates driven by a gtest body; its intended library shell
+ * (include/Builder.hpp:15-35, Gbuilder::Builder<T>) is commented out.  This ABI provides:
+ *   - pg_build_host / pg_build_device: the whole pipeline (Builder::LaunchBuild);
+ *   - one entry point per reference kernel, for callers that drive the stages themselves;
+ *   - readers/writers for the reference's on-disk formats.
+ * Every function returns a pg_status; pg_last_error() gives the message of the calling thread's
+ * last failure.  No function calls exit().  Sizes are runtime values (the reference fixes
+ * N, D and every degree as template parameters).
+ *
+ * Ids are uint32; PG_TOMB (0xFFFFFFFF) marks an empty slot as in the reference
+ * (tests/test_t2iend.cu:674).  Graph outputs are row-major n x degree, tomb padded.
+ */
+#ifndef PARAGRAPH_GB300_H_
+#define PARAGRAPH_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PG_TOMB 0xFFFFFFFFu
+#define PG_ABI_VERSION 1
+
+typedef enum pg_status {
+  PG_OK = 0,
+  PG_EINVAL = 1,       /* bad argument: sizes, ids >= n, misaligned or null pointer */
+  PG_ECUDA = 2,        /* a CUDA call failed */
+  PG_ENOMEM = 3,       /* device or host allocation failed */
+  PG_ETIMEOUT = 4,     /* a search exceeded max_search_iters, or a bounded device wait gave up */
+  PG_EUNSUPPORTED = 5, /* parameter combination outside what the kernels implement */
+  PG_EIO = 6           /* file could not be opened, read or written */
+} pg_status;
+
+typedef enum pg_screen {
+  PG_SCREEN_NONE = 0, /* plain FP32: every distance in the reference's own FP32 order */
+  PG_SCREEN_BF16 = 1, /* BF16 tensor-core screening + exact FP32 re-scoring inside a margin */
+  PG_SCREEN_FP8 = 2   /* FP8 E4M3 per-vector-scaled screening + exact FP32 re-scoring */
+} pg_screen;
+
+/* Build parameters.  pg_params_default() maps (M, L) onto the reference driver's constants
+ * (tests/test_t2iend.cu:671-727): phase 1 keeps gt_k=128, proj_degree=16, proj_pruned=15,
+ * proj_reverse=111; link rounds use pruned = final degree = M and reverse = 128 - 2 - M; the
+ * beam is Km = L - Kp*Kd with Kp=2, Kd=16; reset_iter=15; entry points seed_base + i. */
+typedef struct pg_params {
+  uint32_t gt_k;             /* ground-truth ids per query (columns of gt) */
+  uint32_t proj_degree;      /* out-degree of the projection graph (K3) */
+  uint32_t proj_pruned;      /* phase-1 pruned list length (K2) */
+  uint32_t proj_reverse;     /* phase-1 reverse list length (K2) */
+  uint32_t degree;           /* final out-degree M = link-round pruned length */
+  uint32_t link_reverse;     /* link-round reverse list length */
+  uint32_t link_rounds;      /* search + prune + merge rounds after the projection (2) */
+  uint32_t km;               /* beam: retained list length (Km) */
+  uint32_t kp;               /* beam: nodes expanded per iteration (Kp) */
+  uint32_t kd;               /* beam: neighbours read per expanded node (Kd) */
+  uint32_t reset_iter;       /* the visited set is rebuilt every reset_iter iterations */
+  uint32_t seed_base;        /* search entry points are (seed_base + i) % n, i < Kp*Kd */
+  uint32_t max_search_iters; /* per-query iteration cap; exceeding it returns PG_ETIMEOUT */
+  uint32_t screen;           /* pg_screen */
+  uint32_t flags;            /* PG_FLAG_* */
+  uint32_t reserved[5];
+} pg_params;
+
+/* Ids are always range-checked on the device: an id >= n that is not tomb is replaced by tomb,
+ * never read, and the call returns PG_EINVAL.  The flag is accepted for compatibility. */
+#define PG_FLAG_VALIDATE_INPUT 1u
+
+/* Per-build statistics.  A distance evaluation is one call of the reference's
+ * distance_between (Gbuilder.cuh:785-797) or one search distance (Gsearcher.cuh:1016-1036),
+ * counted as the reference would count it; tomb and visited slots cost nothing. */
+typedef struct pg_stats {
+  uint64_t evals_total;
+  uint64_t evals_proj_prune, evals_proj_merge;
+  uint64_t evals_search[4], evals_prune[4], evals_merge[4];
+  uint64_t search_iters[4];
+  uint64_t rescored[4];      /* screened path: candidates re-scored exactly in FP32 */
+  float ms_total;            /* device time of the whole build (CUDA events) */
+  float ms_proj;             /* K0..K3 */
+  float ms_search[4], ms_prune[4], ms_merge[4];
+  float ms_h2d, ms_d2h;      /* pg_build_host only */
+  uint64_t h2d_bytes, d2h_bytes;
+  uint32_t ep;               /* entry point (most frequent ground-truth id, MatchNN rule) */
+  uint32_t reserved[7];
+} pg_stats;
+
+typedef struct pg_handle_s* pg_handle;
+
+/* ---- library ---------------------------------------------------------------------------- */
+const char* pg_last_error(void);
+uint32_t pg_abi_version(void);
+int pg_params_default(pg_params* p, uint32_t degree, uint32_t beam);
+
+/* A handle owns the device workspace and runs everything on one CUDA stream.  `stream` is a
+ * cudaStream_t (NULL = the legacy default stream).  One build in flight per handle. */
+int pg_create(pg_handle* out, int device, void* stream);
+int pg_destroy(pg_handle h);
+/* Device bytes the handle allocates for a build of n points (the caller can check headroom). */
+int pg_workspace_bytes(const pg_params* p, uint64_t n, uint32_t d, uint64_t q, uint64_t* bytes);
+
+/* ---- whole build (Gbuilder::Builder<float>::LaunchBuild, include/Builder.hpp:15-35) ------- */
+/* Host buffers: copies base (n x d f32) and gt (q x gt_k u32) to the device, builds, copies
+ * the n x degree graph and the n x proj_degree projection back (either may be NULL). */
+int pg_build_host(pg_handle h, const pg_params* p, const float* base, uint64_t n, uint32_t d,
+                  const uint32_t* gt, uint64_t q, uint32_t* graph, uint32_t* proj, pg_stats* st);
+/* Device buffers (resident inputs); outputs are device pointers too (proj may be NULL). */
+int pg_build_device(pg_handle h, const pg_params* p, const float* d_base, uint64_t n,
+                    uint32_t d, const uint32_t* d_gt, uint64_t q, uint32_t* d_graph,
+                    uint32_t* d_proj, pg_stats* st);
+
+/* ---- stages: one entry point per reference kernel, device pointers, handle's stream ------ */
+/* K0 match_top1_kernel_v0 (Gbuilder.cuh:104-135, launched tests/test_t2iend.cu:976): for each
+ * base b that is some query's top-1, row b = gt[w][1..gt_k-2] + 2 tombs where w is the winning
+ * query (the lowest id; canonical form of the atomicCAS race); other rows all tomb.
+ * out: n x gt_k. */
+int pg_match_top1(pg_handle h, const uint32_t* d_gt, uint64_t q, uint32_t gt_k, uint64_t n,
+                  uint32_t* d_out);
+
+/* K1+K2 init_pr_lists + fusion_prune_reverse_kernel_v0 (Gbuilder.cuh:1066-1244, launched
+ * tests/test_t2iend.cu:987-1001,1062-1077): per node, sort its c candidates by distance,
+ * RNG-prune to `pruned`, append reverse edges (ascending source order, first `reverse` kept).
+ * Outputs: pruned list n x pruned + counts n; reverse list n x reverse + counts n (clamped).
+ * d_sorted (optional, n x c) receives each candidate row after the sort, as the reference
+ * sorts the row in place.  evals (optional, host) receives the evaluation count. */
+int pg_prune_reverse(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
+                     const uint32_t* d_graph, uint32_t c, uint32_t pruned, uint32_t reverse,
+                     int strict, uint32_t* d_pruned, uint32_t* d_pruned_num, uint32_t* d_reverse,
+                     uint32_t* d_reverse_num, uint32_t* d_sorted, uint64_t* evals);
+
+/* K3 fusion_merge_sort_prune_kernel (Gbuilder.cuh:1467-1601, launched
+ * tests/test_t2iend.cu:1010,1083,1130): merge reverse + pruned lists, sort, RNG-prune to
+ * `degree`, non-strict fill, tomb padding.  out: n x degree. */
+int pg_merge_prune(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
+                   const uint32_t* d_pruned, const uint32_t* d_pruned_num, uint32_t pruned,
+                   const uint32_t* d_reverse, const uint32_t* d_reverse_num, uint32_t reverse,
+                   uint32_t degree, int strict, uint32_t* d_out, uint64_t* evals);
+
+/* K4 link_process_v0_store_base_data (Gsearcher.cuh:890-1066, launched
+ * tests/test_t2iend.cu:1051,1096): beam search with every base point as the query over the
+ * graph (n x graph_degree).  out: n x (km + kp*kd) ids, parent bit cleared. */
+int pg_search(pg_handle h, const float* d_base, uint64_t n, uint32_t d, const uint32_t* d_graph,
+              uint32_t graph_degree, uint32_t km, uint32_t kp, uint32_t kd, uint32_t reset_iter,
+              uint32_t seed_base, uint32_t max_iters, uint32_t* d_out, uint64_t* evals,
+              uint64_t* iters);
+
+/* ---- on-disk formats ----------------------------------------------------------------------- */
+/* Raw vectors as read by read_vec_from_file (include/utils.hpp:17-35): headerless, exactly
+ * count*elem_size bytes, or with the Big-ANN [u32 n][u32 d] header (README.md:13-21) when
+ * `headered` is non-zero (then rows and cols receive the header). */
+int pg_read_file(const char* path, int headered, void* dst, uint64_t bytes, uint32_t* rows,
+                 uint32_t* cols);
+/* SaveGraph (tests/test_t2iend.cu:615-633): [u32 ep][u32 n] then per node [u32 deg][ids],
+ * deg = number of non-tomb ids of the row, in row order. */
+int pg_save_graph(const char* path, const uint32_t* graph, uint64_t n, uint32_t degree,
+                  uint32_t ep);
+/* ep of MatchNN (tests/test_t2iend.cu:188-221): per query in order, count gt ids up to and
+ * including the first not yet matched one; ep = first id after std::sort by count desc. */
+int pg_entry_point(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint64_t n, uint32_t* ep);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PARAGRAPH_GB300_H_ */

@@ -1,0 +1,772 @@
+// pg_api.cu -- C ABI (include/paragraph_gb300.h): handle, device workspace, the K0..K11
+// pipeline of tests/test_t2iend.cu:974-1139 on one stream, stage entry points, file formats.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/paragraph_gb300.h"
+#include "pg_kernels.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define PG_CUDA(call)                                                                    \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(PG_ECUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                             \
+  } while (0)
+
+constexpr int kMaxRounds = 4;
+constexpr uint32_t kTomb = 0xFFFFFFFFu;
+
+// counters block (device): evals and iterations per stage
+enum Counter {
+  C_PROJ_PRUNE = 0,
+  C_PROJ_MERGE = 1,
+  C_SEARCH = 2,   // + round
+  C_PRUNE = 6,    // + round
+  C_MERGE = 10,   // + round
+  C_ITERS = 14,   // + round
+  C_COUNT = 18
+};
+
+struct Workspace {
+  uint32_t* winner = nullptr;
+  uint32_t* pruned = nullptr;
+  uint32_t* pruned_num = nullptr;
+  uint32_t* indeg = nullptr;
+  uint32_t* offs = nullptr;
+  uint32_t* tile_sums = nullptr;
+  uint32_t* cursor = nullptr;
+  uint32_t* edges = nullptr;
+  uint32_t* rev = nullptr;
+  uint32_t* rev_num = nullptr;
+  uint32_t* sres = nullptr;
+  uint32_t* proj = nullptr;
+  uint32_t* graph = nullptr;
+};
+
+size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
+
+struct Layout {
+  size_t winner, pruned, pruned_num, indeg, offs, tile_sums, cursor, edges, rev, rev_num, sres,
+      proj, graph, total;
+};
+
+Layout make_layout(uint64_t n, uint32_t pmax, uint32_t rmax, uint32_t L, uint32_t proj_deg,
+                   uint32_t degree) {
+  Layout l{};
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = o;
+    o += align_up(bytes);
+    return at;
+  };
+  l.winner = take(n * 4);
+  l.pruned = take(n * pmax * 4);
+  l.pruned_num = take(n * 4);
+  l.indeg = take(n * 4);
+  l.offs = take((n + 1) * 4);
+  l.tile_sums = take(((n + pg::kScanTileElems - 1) / pg::kScanTileElems + 1) * 4);
+  l.cursor = take(n * 4);
+  l.edges = take(n * pmax * 4);
+  l.rev = take(n * rmax * 4);
+  l.rev_num = take(n * 4);
+  l.sres = take(n * L * 4);
+  l.proj = take(n * proj_deg * 4);
+  l.graph = take(n * degree * 4);
+  l.total = o;
+  return l;
+}
+
+}  // namespace
+
+struct pg_handle_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  char* ws = nullptr;
+  size_t ws_bytes = 0;
+  char* inbuf = nullptr;  // device copies of host inputs (pg_build_host)
+  size_t in_bytes = 0;
+  uint32_t* d_status = nullptr;
+  unsigned long long* d_counters = nullptr;
+  uint32_t* d_work = nullptr;
+  uint32_t* h_status = nullptr;  // pinned
+  unsigned long long* h_counters = nullptr;
+  cudaEvent_t ev[16] = {};
+  std::mutex mu;
+};
+
+namespace {
+
+int ensure_ws(pg_handle h, size_t bytes) {
+  if (bytes <= h->ws_bytes) return PG_OK;
+  if (h->ws) cudaFree(h->ws);
+  h->ws = nullptr;
+  h->ws_bytes = 0;
+  cudaError_t e = cudaMalloc(&h->ws, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(PG_ENOMEM, "cudaMalloc of %zu workspace bytes failed: %s", bytes,
+                cudaGetErrorString(e));
+  }
+  h->ws_bytes = bytes;
+  return PG_OK;
+}
+
+int ensure_in(pg_handle h, size_t bytes) {
+  if (bytes <= h->in_bytes) return PG_OK;
+  if (h->inbuf) cudaFree(h->inbuf);
+  h->inbuf = nullptr;
+  h->in_bytes = 0;
+  cudaError_t e = cudaMalloc(&h->inbuf, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(PG_ENOMEM, "cudaMalloc of %zu input bytes failed: %s", bytes,
+                cudaGetErrorString(e));
+  }
+  h->in_bytes = bytes;
+  return PG_OK;
+}
+
+uint32_t pow2_at_least(uint32_t x) {
+  uint32_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+// Visited-set capacity: at most km + reset_iter * kp*kd ids live between rebuilds; twice that
+// (a power of two) keeps the open-addressing table at most half full, so the set stays exact.
+uint32_t hash_slots_for(uint32_t km, uint32_t reset_iter, uint32_t batch) {
+  return pow2_at_least(2 * (km + reset_iter * batch));
+}
+
+int check_params(const pg_params* p, uint64_t n, uint32_t d, uint64_t q) {
+  if (!p) return fail(PG_EINVAL, "params is NULL");
+  if (n == 0 || n >= 0x7FFFFFFFull) return fail(PG_EINVAL, "n=%llu must be in [1, 2^31-1)", (unsigned long long)n);
+  if (q == 0 || q >= 0x7FFFFFFFull) return fail(PG_EINVAL, "q=%llu must be in [1, 2^31-1)", (unsigned long long)q);
+  if (d == 0) return fail(PG_EINVAL, "d must be positive");
+  if (d % 4 != 0) return fail(PG_EUNSUPPORTED, "d=%u: rows must be a multiple of 4 floats", d);
+  if (p->gt_k < 3 || p->gt_k > 128) return fail(PG_EINVAL, "gt_k=%u must be in [3, 128]", p->gt_k);
+  if (p->proj_pruned < 2 || p->proj_pruned > p->gt_k)
+    return fail(PG_EINVAL, "proj_pruned=%u must be in [2, gt_k]", p->proj_pruned);
+  if (p->proj_pruned + p->proj_reverse > 128)
+    return fail(PG_EINVAL, "proj_pruned + proj_reverse must be <= 128");
+  if (p->proj_degree < 2) return fail(PG_EINVAL, "proj_degree must be >= 2");
+  if (p->link_rounds > kMaxRounds) return fail(PG_EINVAL, "link_rounds must be <= %d", kMaxRounds);
+  const uint32_t L = p->km + p->kp * p->kd;
+  if (p->degree < 2 || p->degree > L) return fail(PG_EINVAL, "degree=%u must be in [2, L=%u]", p->degree, L);
+  if (p->degree + p->link_reverse > 128) return fail(PG_EINVAL, "degree + link_reverse must be <= 128");
+  if (p->reset_iter < 1) return fail(PG_EINVAL, "reset_iter must be positive");
+  if (p->link_rounds > 0) {
+    if (!pg::search_supported(d, p->km, p->kp, p->kd))
+      return fail(PG_EUNSUPPORTED,
+                  "search supports kp*kd == 32, km in {32,64,96}, d <= 512 and d %% 4 == 0 "
+                  "(got km=%u kp=%u kd=%u d=%u)", p->km, p->kp, p->kd, d);
+    if (p->kd > p->proj_degree || p->kd > p->degree)
+      return fail(PG_EINVAL, "kd=%u exceeds a graph degree", p->kd);
+  }
+  if (p->screen != PG_SCREEN_NONE)
+    return fail(PG_EUNSUPPORTED, "screened builds are not available in this build");
+  return PG_OK;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+int status_to_error(uint32_t s) {
+  if (s & 4u) return fail(PG_EINVAL, "input holds an id >= n that is not tomb");
+  if (s & 1u) return fail(PG_ETIMEOUT, "a search exceeded max_search_iters");
+  if (s & 2u) return fail(PG_ETIMEOUT, "a bounded device wait gave up");
+  if (s) return fail(PG_ECUDA, "device status 0x%x", s);
+  return PG_OK;
+}
+
+int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, uint32_t d,
+              const uint32_t* gt, uint64_t q, uint32_t* graph_out, uint32_t* proj_out,
+              pg_stats* st) {
+  cudaStream_t s = h->stream;
+  const uint32_t L = p->km + p->kp * p->kd;
+  const uint32_t pmax = std::max(p->proj_pruned, p->degree);
+  const uint32_t rmax = std::max(p->proj_reverse, p->link_reverse);
+  Layout lay = make_layout(n, pmax, rmax, L, p->proj_degree, p->degree);
+  int rc = ensure_ws(h, lay.total);
+  if (rc) return rc;
+  char* w = h->ws;
+  uint32_t* winner = reinterpret_cast<uint32_t*>(w + lay.winner);
+  uint32_t* pruned = reinterpret_cast<uint32_t*>(w + lay.pruned);
+  uint32_t* pnum = reinterpret_cast<uint32_t*>(w + lay.pruned_num);
+  uint32_t* indeg = reinterpret_cast<uint32_t*>(w + lay.indeg);
+  uint32_t* offs = reinterpret_cast<uint32_t*>(w + lay.offs);
+  uint32_t* tsum = reinterpret_cast<uint32_t*>(w + lay.tile_sums);
+  uint32_t* cursor = reinterpret_cast<uint32_t*>(w + lay.cursor);
+  uint32_t* edges = reinterpret_cast<uint32_t*>(w + lay.edges);
+  uint32_t* rev = reinterpret_cast<uint32_t*>(w + lay.rev);
+  uint32_t* rnum = reinterpret_cast<uint32_t*>(w + lay.rev_num);
+  uint32_t* sres = reinterpret_cast<uint32_t*>(w + lay.sres);
+  uint32_t* proj = proj_out ? proj_out : reinterpret_cast<uint32_t*>(w + lay.proj);
+  unsigned long long* cnt = h->d_counters;
+  const int sms = h->num_sms;
+
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(uint32_t), s));
+  PG_CUDA(cudaMemsetAsync(cnt, 0, C_COUNT * sizeof(unsigned long long), s));
+  PG_CUDA(cudaMemsetAsync(h->d_work, 0, 8 * sizeof(uint32_t), s));
+  PG_CUDA(cudaEventRecord(h->ev[0], s));
+
+  // K0 projection winners; K1+K2 phase-1 prune (rows read from gt through the winner)
+  PG_CUDA(pg::launch_match_winner(gt, q, p->gt_k, n, winner, h->d_status, sms, s));
+  PG_CUDA(cudaMemsetAsync(indeg, 0, n * 4, s));
+  pg::PruneArgs pa{};
+  pa.base = base;
+  pa.n = n;
+  pa.d = d;
+  pa.graph = nullptr;
+  pa.c = p->gt_k;
+  pa.gt = gt;
+  pa.winner = winner;
+  pa.gt_k = p->gt_k;
+  pa.p = p->proj_pruned;
+  pa.strict = 0;
+  pa.pruned = pruned;
+  pa.pruned_num = pnum;
+  pa.indeg = indeg;
+  pa.sorted = nullptr;
+  pa.evals = cnt + C_PROJ_PRUNE;
+  pa.status = h->d_status;
+  PG_CUDA(pg::launch_prune_reverse(pa, true, sms, s));
+  PG_CUDA(pg::launch_reverse_csr(pruned, pnum, p->proj_pruned, n, indeg, offs, tsum, cursor, edges,
+                                 sms, s));
+  PG_CUDA(pg::launch_reverse_lists(offs, edges, n, p->proj_reverse, rev, rnum, sms, s));
+  // K3 phase-1 merge -> projection graph
+  pg::MergeArgs ma{};
+  ma.base = base;
+  ma.n = n;
+  ma.d = d;
+  ma.pruned = pruned;
+  ma.pruned_num = pnum;
+  ma.p = p->proj_pruned;
+  ma.reverse = rev;
+  ma.reverse_num = rnum;
+  ma.r = p->proj_reverse;
+  ma.degree = p->proj_degree;
+  ma.strict = 0;
+  ma.out = proj;
+  ma.evals = cnt + C_PROJ_MERGE;
+  ma.status = h->d_status;
+  PG_CUDA(pg::launch_merge_prune(ma, sms, s));
+  PG_CUDA(cudaEventRecord(h->ev[1], s));
+
+  const uint32_t* g = proj;
+  uint32_t gdeg = p->proj_degree;
+  const uint32_t hslots = hash_slots_for(p->km, p->reset_iter, p->kp * p->kd);
+  for (uint32_t r = 0; r < p->link_rounds; r++) {
+    pg::SearchArgs sa{};
+    sa.base = base;
+    sa.n = n;
+    sa.d = d;
+    sa.graph = g;
+    sa.graph_degree = gdeg;
+    sa.km = p->km;
+    sa.kp = p->kp;
+    sa.kd = p->kd;
+    sa.reset_iter = p->reset_iter;
+    sa.seed_base = p->seed_base;
+    sa.max_iters = p->max_search_iters;
+    sa.order = nullptr;
+    sa.out = sres;
+    sa.evals = cnt + C_SEARCH + r;
+    sa.iters = cnt + C_ITERS + r;
+    sa.work = h->d_work + r;
+    sa.status = h->d_status;
+    sa.hash_slots = hslots;
+    PG_CUDA(pg::launch_search(sa, sms, h->smem_optin, s));
+    PG_CUDA(cudaEventRecord(h->ev[2 + 3 * r], s));
+    PG_CUDA(cudaMemsetAsync(indeg, 0, n * 4, s));
+    pg::PruneArgs pr{};
+    pr.base = base;
+    pr.n = n;
+    pr.d = d;
+    pr.graph = sres;
+    pr.c = L;
+    pr.p = p->degree;
+    pr.strict = 1;
+    pr.pruned = pruned;
+    pr.pruned_num = pnum;
+    pr.indeg = indeg;
+    pr.sorted = nullptr;
+    pr.evals = cnt + C_PRUNE + r;
+    pr.status = h->d_status;
+    PG_CUDA(pg::launch_prune_reverse(pr, false, sms, s));
+    PG_CUDA(pg::launch_reverse_csr(pruned, pnum, p->degree, n, indeg, offs, tsum, cursor, edges,
+                                   sms, s));
+    PG_CUDA(pg::launch_reverse_lists(offs, edges, n, p->link_reverse, rev, rnum, sms, s));
+    PG_CUDA(cudaEventRecord(h->ev[3 + 3 * r], s));
+    pg::MergeArgs mr{};
+    mr.base = base;
+    mr.n = n;
+    mr.d = d;
+    mr.pruned = pruned;
+    mr.pruned_num = pnum;
+    mr.p = p->degree;
+    mr.reverse = rev;
+    mr.reverse_num = rnum;
+    mr.r = p->link_reverse;
+    mr.degree = p->degree;
+    mr.strict = 1;
+    mr.out = graph_out;
+    mr.evals = cnt + C_MERGE + r;
+    mr.status = h->d_status;
+    PG_CUDA(pg::launch_merge_prune(mr, sms, s));
+    PG_CUDA(cudaEventRecord(h->ev[4 + 3 * r], s));
+    g = graph_out;
+    gdeg = p->degree;
+  }
+  if (p->link_rounds == 0 && graph_out) {
+    // no link rounds: the projection is the graph (degree columns, tomb padded)
+    PG_CUDA(cudaMemset2DAsync(graph_out, p->degree * 4, 0xFF, p->degree * 4, n, s));
+    PG_CUDA(cudaMemcpy2DAsync(graph_out, p->degree * 4, proj, p->proj_degree * 4,
+                              std::min(p->degree, p->proj_degree) * 4, n,
+                              cudaMemcpyDeviceToDevice, s));
+  }
+  PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_counters, cnt, C_COUNT * 8, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  rc = status_to_error(*h->h_status);
+  if (rc) return rc;
+  if (st) {
+    const unsigned long long* c = h->h_counters;
+    st->evals_proj_prune = c[C_PROJ_PRUNE];
+    st->evals_proj_merge = c[C_PROJ_MERGE];
+    st->evals_total = c[C_PROJ_PRUNE] + c[C_PROJ_MERGE];
+    for (int r = 0; r < kMaxRounds; r++) {
+      st->evals_search[r] = c[C_SEARCH + r];
+      st->evals_prune[r] = c[C_PRUNE + r];
+      st->evals_merge[r] = c[C_MERGE + r];
+      st->search_iters[r] = c[C_ITERS + r];
+      st->evals_total += c[C_SEARCH + r] + c[C_PRUNE + r] + c[C_MERGE + r];
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+    st->ms_proj = ms;
+    cudaEvent_t prev = h->ev[1];
+    for (uint32_t r = 0; r < p->link_rounds; r++) {
+      cudaEventElapsedTime(&st->ms_search[r], prev, h->ev[2 + 3 * r]);
+      cudaEventElapsedTime(&st->ms_prune[r], h->ev[2 + 3 * r], h->ev[3 + 3 * r]);
+      cudaEventElapsedTime(&st->ms_merge[r], h->ev[3 + 3 * r], h->ev[4 + 3 * r]);
+      prev = h->ev[4 + 3 * r];
+    }
+    cudaEventElapsedTime(&st->ms_total, h->ev[0], prev);
+  }
+  return PG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pg_last_error(void) { return g_err.c_str(); }
+
+uint32_t pg_abi_version(void) { return PG_ABI_VERSION; }
+
+int pg_params_default(pg_params* p, uint32_t degree, uint32_t beam) {
+  if (!p) return fail(PG_EINVAL, "params is NULL");
+  if (degree < 2 || degree > 126) return fail(PG_EINVAL, "degree=%u must be in [2, 126]", degree);
+  const uint32_t kp = 2, kd = 16;
+  if (beam <= kp * kd) return fail(PG_EINVAL, "beam=%u must exceed kp*kd=%u", beam, kp * kd);
+  std::memset(p, 0, sizeof(*p));
+  p->gt_k = 128;
+  p->proj_degree = 16;
+  p->proj_pruned = 15;
+  p->proj_reverse = 111;
+  p->degree = degree;
+  p->link_reverse = 128 - 2 - degree;
+  p->link_rounds = 2;
+  p->km = beam - kp * kd;
+  p->kp = kp;
+  p->kd = kd;
+  p->reset_iter = 15;
+  p->seed_base = 3030517;
+  p->max_search_iters = 1u << 20;
+  p->screen = PG_SCREEN_NONE;
+  p->flags = 0;
+  return PG_OK;
+}
+
+int pg_create(pg_handle* out, int device, void* stream) {
+  if (!out) return fail(PG_EINVAL, "out is NULL");
+  *out = nullptr;
+  int count = 0;
+  PG_CUDA(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count) return fail(PG_EINVAL, "device %d of %d", device, count);
+  PG_CUDA(cudaSetDevice(device));
+  pg_handle h = new (std::nothrow) pg_handle_s();
+  if (!h) return fail(PG_ENOMEM, "host allocation failed");
+  h->device = device;
+  h->stream = static_cast<cudaStream_t>(stream);
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, device);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_status, 64);
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_counters, 64 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&h->d_work, 64);
+  if (e == cudaSuccess) e = cudaMallocHost(&h->h_status, 64);
+  if (e == cudaSuccess) e = cudaMallocHost(&h->h_counters, 64 * sizeof(unsigned long long));
+  for (int i = 0; i < 16 && e == cudaSuccess; i++) e = cudaEventCreate(&h->ev[i]);
+  if (e != cudaSuccess) {
+    pg_destroy(h);
+    return fail(PG_ECUDA, "pg_create: %s", cudaGetErrorString(e));
+  }
+  h->num_sms = prop.multiProcessorCount;
+  h->smem_optin = prop.sharedMemPerBlockOptin;
+  *out = h;
+  return PG_OK;
+}
+
+int pg_destroy(pg_handle h) {
+  if (!h) return PG_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->ws);
+  cudaFree(h->inbuf);
+  cudaFree(h->d_status);
+  cudaFree(h->d_counters);
+  cudaFree(h->d_work);
+  cudaFreeHost(h->h_status);
+  cudaFreeHost(h->h_counters);
+  for (int i = 0; i < 16; i++)
+    if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+  delete h;
+  return PG_OK;
+}
+
+int pg_workspace_bytes(const pg_params* p, uint64_t n, uint32_t d, uint64_t q, uint64_t* bytes) {
+  int rc = check_params(p, n, d, q);
+  if (rc) return rc;
+  if (!bytes) return fail(PG_EINVAL, "bytes is NULL");
+  const uint32_t L = p->km + p->kp * p->kd;
+  Layout l = make_layout(n, std::max(p->proj_pruned, p->degree),
+                         std::max(p->proj_reverse, p->link_reverse), L, p->proj_degree, p->degree);
+  *bytes = l.total;
+  return PG_OK;
+}
+
+int pg_build_device(pg_handle h, const pg_params* p, const float* d_base, uint64_t n, uint32_t d,
+                    const uint32_t* d_gt, uint64_t q, uint32_t* d_graph, uint32_t* d_proj,
+                    pg_stats* st) {
+  if (!h) return fail(PG_EINVAL, "handle is NULL");
+  int rc = check_params(p, n, d, q);
+  if (rc) return rc;
+  if (!d_base || !d_gt) return fail(PG_EINVAL, "base and gt must be device pointers");
+  if (p->link_rounds > 0 && !d_graph) return fail(PG_EINVAL, "graph output is NULL");
+  if (!aligned16(d_base)) return fail(PG_EINVAL, "base must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  if (st) std::memset(st, 0, sizeof(*st));
+  return run_build(h, p, d_base, n, d, d_gt, q, d_graph, d_proj, st);
+}
+
+int pg_build_host(pg_handle h, const pg_params* p, const float* base, uint64_t n, uint32_t d,
+                  const uint32_t* gt, uint64_t q, uint32_t* graph, uint32_t* proj, pg_stats* st) {
+  if (!h) return fail(PG_EINVAL, "handle is NULL");
+  int rc = check_params(p, n, d, q);
+  if (rc) return rc;
+  if (!base || !gt) return fail(PG_EINVAL, "base and gt are NULL");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  const size_t bb = align_up(n * d * 4), gb = align_up(q * p->gt_k * 4);
+  const size_t ob = align_up(n * p->degree * 4), pb = align_up(n * p->proj_degree * 4);
+  rc = ensure_in(h, bb + gb + ob + pb);
+  if (rc) return rc;
+  float* d_base = reinterpret_cast<float*>(h->inbuf);
+  uint32_t* d_gt = reinterpret_cast<uint32_t*>(h->inbuf + bb);
+  uint32_t* d_graph = reinterpret_cast<uint32_t*>(h->inbuf + bb + gb);
+  uint32_t* d_proj = reinterpret_cast<uint32_t*>(h->inbuf + bb + gb + ob);
+  cudaStream_t s = h->stream;
+  cudaEvent_t t0, t1, t2, t3;
+  PG_CUDA(cudaEventCreate(&t0));
+  PG_CUDA(cudaEventCreate(&t1));
+  PG_CUDA(cudaEventCreate(&t2));
+  PG_CUDA(cudaEventCreate(&t3));
+  PG_CUDA(cudaEventRecord(t0, s));
+  PG_CUDA(cudaMemcpyAsync(d_base, base, n * d * 4, cudaMemcpyHostToDevice, s));
+  PG_CUDA(cudaMemcpyAsync(d_gt, gt, q * p->gt_k * 4, cudaMemcpyHostToDevice, s));
+  PG_CUDA(cudaEventRecord(t1, s));
+  if (st) std::memset(st, 0, sizeof(*st));
+  rc = run_build(h, p, d_base, n, d, d_gt, q, d_graph, d_proj, st);
+  if (rc) {
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    cudaEventDestroy(t2);
+    cudaEventDestroy(t3);
+    return rc;
+  }
+  PG_CUDA(cudaEventRecord(t2, s));
+  uint64_t d2h = 0;
+  if (graph && p->link_rounds > 0) {
+    PG_CUDA(cudaMemcpyAsync(graph, d_graph, n * p->degree * 4, cudaMemcpyDeviceToHost, s));
+    d2h += n * p->degree * 4;
+  }
+  if (proj) {
+    PG_CUDA(cudaMemcpyAsync(proj, d_proj, n * p->proj_degree * 4, cudaMemcpyDeviceToHost, s));
+    d2h += n * p->proj_degree * 4;
+  }
+  PG_CUDA(cudaEventRecord(t3, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  if (st) {
+    cudaEventElapsedTime(&st->ms_h2d, t0, t1);
+    cudaEventElapsedTime(&st->ms_d2h, t2, t3);
+    st->h2d_bytes = n * d * 4 + q * p->gt_k * 4;
+    st->d2h_bytes = d2h;
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaEventDestroy(t2);
+  cudaEventDestroy(t3);
+  return PG_OK;
+}
+
+// ---------------------------------------------------------------- stage entry points
+
+int pg_match_top1(pg_handle h, const uint32_t* d_gt, uint64_t q, uint32_t gt_k, uint64_t n,
+                  uint32_t* d_out) {
+  if (!h || !d_gt || !d_out) return fail(PG_EINVAL, "NULL argument");
+  if (gt_k < 3 || n == 0 || n >= 0x7FFFFFFFull || q >= 0x7FFFFFFFull)
+    return fail(PG_EINVAL, "bad sizes");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  int rc = ensure_ws(h, align_up(n * 4));
+  if (rc) return rc;
+  uint32_t* winner = reinterpret_cast<uint32_t*>(h->ws);
+  cudaStream_t s = h->stream;
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, s));
+  PG_CUDA(pg::launch_match_winner(d_gt, q, gt_k, n, winner, h->d_status, h->num_sms, s));
+  PG_CUDA(pg::launch_match_rows(d_gt, gt_k, n, winner, d_out, h->num_sms, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  return status_to_error(*h->h_status);
+}
+
+int pg_prune_reverse(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
+                     const uint32_t* d_graph, uint32_t c, uint32_t pruned, uint32_t reverse,
+                     int strict, uint32_t* d_pruned, uint32_t* d_pruned_num, uint32_t* d_reverse,
+                     uint32_t* d_reverse_num, uint32_t* d_sorted, uint64_t* evals) {
+  if (!h || !d_base || !d_graph || !d_pruned || !d_pruned_num || !d_reverse || !d_reverse_num)
+    return fail(PG_EINVAL, "NULL argument");
+  if (n == 0 || n >= 0x7FFFFFFFull || d == 0) return fail(PG_EINVAL, "bad sizes");
+  if (d % 4 != 0 || !aligned16(d_base)) return fail(PG_EUNSUPPORTED, "d %% 4 != 0 or unaligned base");
+  if (c < 1 || c > 128) return fail(PG_EINVAL, "c=%u must be in [1, 128]", c);
+  if (pruned < 2 || pruned > c) return fail(PG_EINVAL, "pruned=%u must be in [2, c]", pruned);
+  if (reverse > 128) return fail(PG_EINVAL, "reverse must be <= 128");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  const size_t tiles = (n + pg::kScanTileElems - 1) / pg::kScanTileElems + 1;
+  const size_t b_indeg = align_up(n * 4), b_offs = align_up((n + 1) * 4),
+               b_tiles = align_up(tiles * 4), b_cursor = align_up(n * 4),
+               b_edges = align_up(n * pruned * 4);
+  int rc = ensure_ws(h, b_indeg + b_offs + b_tiles + b_cursor + b_edges);
+  if (rc) return rc;
+  char* w = h->ws;
+  uint32_t* indeg = reinterpret_cast<uint32_t*>(w);
+  uint32_t* offs = reinterpret_cast<uint32_t*>(w + b_indeg);
+  uint32_t* tsum = reinterpret_cast<uint32_t*>(w + b_indeg + b_offs);
+  uint32_t* cursor = reinterpret_cast<uint32_t*>(w + b_indeg + b_offs + b_tiles);
+  uint32_t* edges = reinterpret_cast<uint32_t*>(w + b_indeg + b_offs + b_tiles + b_cursor);
+  cudaStream_t s = h->stream;
+  PG_CUDA(cudaMemsetAsync(h->d_counters, 0, 8, s));
+  PG_CUDA(cudaMemsetAsync(indeg, 0, n * 4, s));
+  pg::PruneArgs a{};
+  a.base = d_base;
+  a.n = n;
+  a.d = d;
+  a.graph = d_graph;
+  a.c = c;
+  a.p = pruned;
+  a.strict = strict;
+  a.pruned = d_pruned;
+  a.pruned_num = d_pruned_num;
+  a.indeg = indeg;
+  a.sorted = d_sorted;
+  a.evals = h->d_counters;
+  a.status = h->d_status;
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, s));
+  PG_CUDA(pg::launch_prune_reverse(a, false, h->num_sms, s));
+  PG_CUDA(pg::launch_reverse_csr(d_pruned, d_pruned_num, pruned, n, indeg, offs, tsum, cursor,
+                                 edges, h->num_sms, s));
+  PG_CUDA(pg::launch_reverse_lists(offs, edges, n, reverse, d_reverse, d_reverse_num, h->num_sms, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_counters, h->d_counters, 8, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  if (evals) *evals = h->h_counters[0];
+  return status_to_error(*h->h_status);
+}
+
+int pg_merge_prune(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
+                   const uint32_t* d_pruned, const uint32_t* d_pruned_num, uint32_t pruned,
+                   const uint32_t* d_reverse, const uint32_t* d_reverse_num, uint32_t reverse,
+                   uint32_t degree, int strict, uint32_t* d_out, uint64_t* evals) {
+  if (!h || !d_base || !d_pruned || !d_pruned_num || !d_reverse || !d_reverse_num || !d_out)
+    return fail(PG_EINVAL, "NULL argument");
+  if (n == 0 || n >= 0x7FFFFFFFull || d == 0) return fail(PG_EINVAL, "bad sizes");
+  if (d % 4 != 0 || !aligned16(d_base)) return fail(PG_EUNSUPPORTED, "d %% 4 != 0 or unaligned base");
+  if (pruned + reverse > 128 || degree < 2)
+    return fail(PG_EINVAL, "pruned + reverse must be <= 128 and degree >= 2");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  cudaStream_t s = h->stream;
+  PG_CUDA(cudaMemsetAsync(h->d_counters, 0, 8, s));
+  pg::MergeArgs a{};
+  a.base = d_base;
+  a.n = n;
+  a.d = d;
+  a.pruned = d_pruned;
+  a.pruned_num = d_pruned_num;
+  a.p = pruned;
+  a.reverse = d_reverse;
+  a.reverse_num = d_reverse_num;
+  a.r = reverse;
+  a.degree = degree;
+  a.strict = strict;
+  a.out = d_out;
+  a.evals = h->d_counters;
+  a.status = h->d_status;
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, s));
+  PG_CUDA(pg::launch_merge_prune(a, h->num_sms, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_counters, h->d_counters, 8, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  if (evals) *evals = h->h_counters[0];
+  return status_to_error(*h->h_status);
+}
+
+int pg_search(pg_handle h, const float* d_base, uint64_t n, uint32_t d, const uint32_t* d_graph,
+              uint32_t graph_degree, uint32_t km, uint32_t kp, uint32_t kd, uint32_t reset_iter,
+              uint32_t seed_base, uint32_t max_iters, uint32_t* d_out, uint64_t* evals,
+              uint64_t* iters) {
+  if (!h || !d_base || !d_graph || !d_out) return fail(PG_EINVAL, "NULL argument");
+  if (n == 0 || n >= 0x7FFFFFFFull) return fail(PG_EINVAL, "bad n");
+  if (!pg::search_supported(d, km, kp, kd))
+    return fail(PG_EUNSUPPORTED, "search supports kp*kd == 32, km in {32,64,96}, d <= 512, d %% 4 == 0");
+  if (kd > graph_degree) return fail(PG_EINVAL, "kd exceeds graph_degree");
+  if (reset_iter < 1) return fail(PG_EINVAL, "reset_iter must be positive");
+  if (!aligned16(d_base)) return fail(PG_EINVAL, "base must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  cudaStream_t s = h->stream;
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, s));
+  PG_CUDA(cudaMemsetAsync(h->d_counters, 0, 16, s));
+  PG_CUDA(cudaMemsetAsync(h->d_work, 0, 4, s));
+  pg::SearchArgs a{};
+  a.base = d_base;
+  a.n = n;
+  a.d = d;
+  a.graph = d_graph;
+  a.graph_degree = graph_degree;
+  a.km = km;
+  a.kp = kp;
+  a.kd = kd;
+  a.reset_iter = reset_iter;
+  a.seed_base = seed_base;
+  a.max_iters = max_iters;
+  a.order = nullptr;
+  a.out = d_out;
+  a.evals = h->d_counters;
+  a.iters = h->d_counters + 1;
+  a.work = h->d_work;
+  a.status = h->d_status;
+  a.hash_slots = hash_slots_for(km, reset_iter, kp * kd);
+  PG_CUDA(pg::launch_search(a, h->num_sms, h->smem_optin, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_counters, h->d_counters, 16, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  if (evals) *evals = h->h_counters[0];
+  if (iters) *iters = h->h_counters[1];
+  return status_to_error(*h->h_status);
+}
+
+// ---------------------------------------------------------------- file formats
+
+int pg_read_file(const char* path, int headered, void* dst, uint64_t bytes, uint32_t* rows,
+                 uint32_t* cols) {
+  if (!path || (!dst && bytes)) return fail(PG_EINVAL, "NULL argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(PG_EIO, "cannot open %s", path);
+  if (headered) {
+    uint32_t hdr[2];
+    if (std::fread(hdr, 4, 2, f) != 2) {
+      std::fclose(f);
+      return fail(PG_EIO, "%s: short header", path);
+    }
+    if (rows) *rows = hdr[0];
+    if (cols) *cols = hdr[1];
+  }
+  size_t got = bytes ? std::fread(dst, 1, bytes, f) : 0;
+  std::fclose(f);
+  if (got != bytes)
+    return fail(PG_EIO, "%s: read %zu of %llu bytes", path, got, (unsigned long long)bytes);
+  return PG_OK;
+}
+
+int pg_save_graph(const char* path, const uint32_t* graph, uint64_t n, uint32_t degree,
+                  uint32_t ep) {
+  if (!path || (!graph && n)) return fail(PG_EINVAL, "NULL argument");
+  if (n > 0xFFFFFFFFull) return fail(PG_EINVAL, "n does not fit the u32 header");
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(PG_EIO, "cannot open %s for writing", path);
+  uint32_t hdr[2] = {ep, static_cast<uint32_t>(n)};
+  bool ok = std::fwrite(hdr, 4, 2, f) == 2;
+  std::vector<uint32_t> row(static_cast<size_t>(degree) + 1);
+  for (uint64_t i = 0; ok && i < n; i++) {
+    uint32_t k = 0;
+    for (uint32_t j = 0; j < degree; j++) {
+      const uint32_t v = graph[i * degree + j];
+      if (v != kTomb) row[1 + k++] = v;
+    }
+    row[0] = k;
+    ok = std::fwrite(row.data(), 4, k + 1, f) == k + 1;
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? PG_OK : fail(PG_EIO, "write to %s failed", path);
+}
+
+int pg_entry_point(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint64_t n, uint32_t* ep) {
+  if (!gt || !ep || n == 0) return fail(PG_EINVAL, "NULL argument");
+  std::vector<uint32_t> freq(n, 0);
+  std::vector<bool> vis(n, false);
+  for (uint64_t qi = 0; qi < q; qi++) {
+    bool matched = false;
+    for (uint32_t j = 0; j < gt_k; j++) {
+      const uint32_t nn = gt[qi * gt_k + j];
+      if (nn >= n || matched) break;
+      ++freq[nn];
+      if (vis[nn]) continue;
+      vis[nn] = true;
+      matched = true;
+    }
+  }
+  std::vector<uint32_t> order(n);
+  std::iota(order.begin(), order.end(), 0u);
+  std::sort(order.begin(), order.end(),
+            [&](uint32_t a, uint32_t b) { return freq[a] > freq[b]; });
+  *ep = order[0];
+  return PG_OK;
+}
+
+}  // extern "C"

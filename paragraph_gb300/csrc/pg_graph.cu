@@ -1,0 +1,595 @@
+// pg_graph.cu -- projection (K0), prune + reverse edges (K1/K2), reverse lists, merge (K3).
+//
+// Layout in HBM (all row-major, 64-bit row offsets):
+//   base      n x d f32               the vectors (read-only)
+//   winner    n u32                   projection winner key per base (K0)
+//   pruned    n x P u32 + n counts    RNG-pruned out-lists (K2)
+//   indeg     n u32 -> offs n+1       reverse-edge counts -> CSR offsets
+//   edges     sum(pruned counts) u32  reverse sources grouped by destination (CSR)
+//   reverse   n x R u32 + n counts    first R sources per destination, ascending (K2's add_reverse)
+//   graph     n x degree u32          merged + pruned out-lists, tomb padded (K3)
+// One warp owns one node in K2, the reverse-list finish and K3; lanes split candidates for the
+// distance pass and kept entries for the occlusion tests.  Every distance is one FMA chain in
+// d order (dist_seq), the reference's distance_between, so ids are bit-identical to it.
+#include "pg_device.cuh"
+#include "pg_kernels.h"
+
+namespace pg {
+
+// ------------------------------------------------------------------ K0: projection winners
+// Winner key of query q for its top-1 base: queries whose gt[q][1] is a real id compete by
+// lowest id; a query whose gt[q][1] is tomb leaves the CAS slot of match_top1_kernel_v0
+// (Gbuilder.cuh:122) at tomb, so a later query overwrites its row: among those the highest id
+// is the last writer.  Real-id queries always win over tomb ones.
+__device__ __forceinline__ uint32_t winner_key(uint32_t q, bool real_first) {
+  return real_first ? q : 0x80000000u + (0x7FFFFFFEu - q);
+}
+__device__ __forceinline__ uint32_t winner_query(uint32_t key) {
+  if (key == kTomb) return kTomb;
+  return key < 0x80000000u ? key : 0x7FFFFFFEu - (key - 0x80000000u);
+}
+
+__global__ void k_match_winner(const uint32_t* __restrict__ gt, uint64_t q, uint32_t gt_k,
+                               uint64_t n, uint32_t* __restrict__ winner, uint32_t* status) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t qi = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; qi < q;
+       qi += stride) {
+    const uint32_t b = gt[qi * gt_k];
+    if (b == kTomb) continue;
+    if (b >= n) {
+      raise_error(status, kErrBadId);
+      continue;
+    }
+    const bool real = gt[qi * gt_k + 1] != kTomb;
+    atomicMin(winner + b, winner_key(static_cast<uint32_t>(qi), real));
+  }
+}
+
+// Materialises the n x gt_k projection rows of match_top1_kernel_v0 (stage API only; the build
+// reads gt through `winner` directly): row b = gt[w][1..gt_k-2] followed by two tombs.
+__global__ void k_match_rows(const uint32_t* __restrict__ gt, uint32_t gt_k, uint64_t n,
+                             const uint32_t* __restrict__ winner, uint32_t* __restrict__ out) {
+  const uint64_t total = n * gt_k;
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += stride) {
+    const uint64_t b = i / gt_k;
+    const uint32_t j = static_cast<uint32_t>(i - b * gt_k);
+    const uint32_t w = winner_query(winner[b]);
+    out[i] = (w != kTomb && j + 2 < gt_k) ? gt[static_cast<uint64_t>(w) * gt_k + j + 1] : kTomb;
+  }
+}
+
+__global__ void k_validate_ids(const uint32_t* __restrict__ ids, uint64_t count, uint64_t n,
+                               uint32_t* status) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  bool bad = false;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < count;
+       i += stride) {
+    const uint32_t v = ids[i];
+    bad |= (v != kTomb && v >= n);
+  }
+  if (__any_sync(kFull, bad) && lane_id() == 0) raise_error(status, kErrBadId);
+}
+
+// ------------------------------------------------------------------ distances, E per lane
+// E independent FMA chains (one per candidate slot of this lane), interleaved for ILP.  Slots
+// with valid[s] == false are skipped and return FLT_MAX.
+template <int E>
+__device__ __forceinline__ void dist_seq_multi(const float* __restrict__ brow,
+                                               const float* __restrict__ base, uint32_t d,
+                                               const uint32_t (&id)[E], const bool (&valid)[E],
+                                               float (&out)[E]) {
+  float s[E];
+  const float4* rows[E];
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    s[e] = 0.0f;
+    rows[e] = reinterpret_cast<const float4*>(valid[e] ? base + static_cast<uint64_t>(id[e]) * d
+                                                       : brow);
+  }
+  const float4* b4 = reinterpret_cast<const float4*>(brow);
+  const uint32_t n4 = d >> 2;
+#pragma unroll 2
+  for (uint32_t i = 0; i < n4; i++) {
+    const float4 u = __ldg(b4 + i);
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const float4 v = __ldg(rows[e] + i);
+      s[e] = fmaf(u.x, v.x, s[e]);
+      s[e] = fmaf(u.y, v.y, s[e]);
+      s[e] = fmaf(u.z, v.z, s[e]);
+      s[e] = fmaf(u.w, v.w, s[e]);
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < E; e++) out[e] = valid[e] ? -s[e] : FLT_MAX;
+}
+
+// Occlusion test of candidate p (distance dp to the node) against kept[0..k] in order
+// (Gbuilder.cuh:1163-1181): true if some kept r has dist(p, r) < dp.  Lanes test 32 kept entries
+// at a time; *checks gets the number of comparisons the reference makes (up to the first hit).
+__device__ __forceinline__ bool occluded(const float* __restrict__ base, uint64_t n, uint32_t d,
+                                         uint32_t p, float dp, const uint32_t* kept, uint32_t k,
+                                         uint64_t* checks) {
+  const uint32_t lane = lane_id();
+  if (p >= n) return true;  // only reachable after an input error was flagged
+  const float* prow = base + static_cast<uint64_t>(p) * d;
+  for (uint32_t t0 = 0; t0 <= k; t0 += 32) {
+    const uint32_t t = t0 + lane;
+    bool o = false;
+    if (t <= k && kept[t] < n) o = dist_seq(prow, base + static_cast<uint64_t>(kept[t]) * d, d) < dp;
+    const unsigned m = __ballot_sync(kFull, o);
+    if (m) {
+      *checks += static_cast<uint32_t>(__ffs(static_cast<int>(m)));
+      return true;
+    }
+    *checks += min(32u, k + 1 - t0);
+  }
+  return false;
+}
+
+__device__ __forceinline__ float key_dist(uint64_t key) {
+  const uint32_t o = static_cast<uint32_t>(key >> 32);
+  const uint32_t u = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
+  return __uint_as_float(u);
+}
+
+// ------------------------------------------------------------------ K2: prune + reverse
+// fusion_prune_reverse_kernel_v0 (Gbuilder.cuh:1093-1244).  PHASE1 reads the candidate row of
+// node b straight from the winner's ground truth (the K0 row) instead of a materialised graph.
+template <int E, bool PHASE1>
+__global__ void __launch_bounds__(256) k_prune_reverse(PruneArgs a) {
+  constexpr int C_MAX = 32 * E;
+  extern __shared__ uint32_t smem_u32[];
+  const uint32_t lane = lane_id();
+  const uint32_t warp = threadIdx.x >> 5;
+  uint32_t* ids_s = smem_u32 + warp * (3 * C_MAX);
+  float* dist_s = reinterpret_cast<float*>(ids_s + C_MAX);
+  uint32_t* kept_s = ids_s + 2 * C_MAX;
+  const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (blockDim.x >> 5);
+  uint64_t ev = 0;
+  for (uint64_t b = blockIdx.x * static_cast<uint64_t>(blockDim.x >> 5) + warp; b < a.n;
+       b += nwarps) {
+    uint32_t id[E];
+    bool valid[E];
+    uint32_t w = kTomb;
+    if (PHASE1) w = winner_query(a.winner[b]);
+    if (PHASE1 && w == kTomb) {  // nobody's top-1: an all-tomb row, nothing kept
+      if (lane == 0) a.pruned_num[b] = 0;
+      if (a.sorted)
+        for (uint32_t j = lane; j < a.c; j += 32) a.sorted[b * a.c + j] = kTomb;
+      continue;
+    }
+#pragma unroll
+    for (int s = 0; s < E; s++) {
+      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+      uint32_t x = kTomb;
+      if (j < a.c) {
+        if (PHASE1)
+          x = (j + 2 < a.gt_k) ? a.gt[static_cast<uint64_t>(w) * a.gt_k + j + 1] : kTomb;
+        else
+          x = a.graph[b * a.c + j];
+      }
+      if (x >= a.n && x != kTomb && x != kMaskedTomb) {  // out-of-range input id
+        raise_error(a.status, kErrBadId);
+        x = kTomb;
+      }
+      id[s] = x;
+      valid[s] = (x != kTomb && x != static_cast<uint32_t>(b) && x != kMaskedTomb);
+    }
+    float dist[E];
+    dist_seq_multi<E>(a.base + b * a.d, a.base, a.d, id, valid, dist);
+    uint64_t key[E];
+#pragma unroll
+    for (int s = 0; s < E; s++) {
+      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+      ev += __popc(__ballot_sync(kFull, valid[s])) * (lane == 0);
+      key[s] = (j < a.c) ? pack_key(dist[s], j) : ~0ull;
+    }
+    warp_sort_kv<E>(key, id);
+#pragma unroll
+    for (int s = 0; s < E; s++) {
+      const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
+      if (i < a.c) {
+        ids_s[i] = id[s];
+        dist_s[i] = key_dist(key[s]);
+        if (a.sorted) a.sorted[b * a.c + i] = id[s];
+      }
+    }
+    __syncwarp();
+    const uint32_t first = ids_s[0];
+    if (first == kTomb || first == kMaskedTomb) {
+      if (lane == 0) a.pruned_num[b] = 0;
+      __syncwarp();
+      continue;
+    }
+    if (lane == 0) kept_s[0] = first;
+    __syncwarp();
+    uint32_t k = 0;
+    uint32_t j = 1;
+    uint64_t checks = 0;
+    for (; j < a.c; j++) {
+      const uint32_t p = ids_s[j];
+      if (p == kTomb || p == kMaskedTomb) break;
+      if (!occluded(a.base, a.n, a.d, p, dist_s[j], kept_s, k, &checks)) {
+        k++;
+        if (lane == 0) kept_s[k] = p;
+        __syncwarp();
+        if (k == a.p - 1) break;
+      }
+    }
+    if (!a.strict && k < a.p - 1) {  // non-strict fill (Gbuilder.cuh:1201-1239)
+      for (uint32_t j2 = j; j2 < a.c && k < a.p - 1; j2++) {
+        const uint32_t x = ids_s[j2];
+        if (x == kTomb || x == static_cast<uint32_t>(b) || x == kMaskedTomb) continue;
+        bool dup = false;
+        for (uint32_t t0 = 0; t0 <= k; t0 += 32) {
+          const uint32_t t = t0 + lane;
+          dup |= __any_sync(kFull, t <= k && kept_s[t] == x);
+        }
+        if (!dup) {
+          k++;
+          if (lane == 0) kept_s[k] = x;
+          __syncwarp();
+        }
+      }
+    }
+    ev += (lane == 0) ? checks : 0;
+    const uint32_t cnt = k + 1;
+    if (lane == 0) a.pruned_num[b] = cnt;
+    for (uint32_t t = lane; t < cnt; t += 32) {
+      const uint32_t dst = kept_s[t];
+      a.pruned[b * a.p + t] = dst;
+      atomicAdd(a.indeg + dst, 1u);
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && ev) atomicAdd(a.evals, static_cast<unsigned long long>(ev));
+}
+
+// ------------------------------------------------------------------ reverse edges (CSR)
+// Exclusive scan of n counts into offs[0..n] (offs[n] = total).  Three passes: per-block sums,
+// one block scanning the block sums, per-block scan plus offset.
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums,
+                                                         uint32_t* total) {
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, x, o);
+    if (lane >= static_cast<uint32_t>(o)) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = (lane < (blockDim.x >> 5)) ? warp_sums[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, w, o);
+      if (lane >= static_cast<uint32_t>(o)) w += y;
+    }
+    warp_sums[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t before = (warp ? warp_sums[warp - 1] : 0) + x - v;
+  if (total) *total = warp_sums[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return before;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32_t* __restrict__ in,
+                                                             uint64_t n,
+                                                             uint32_t* __restrict__ tile_sums) {
+  __shared__ uint32_t ws[32];
+  const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; i++) s += (base + i < n) ? in[base + i] : 0u;
+  uint32_t total;
+  block_exclusive_scan(s, ws, &total);
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(uint32_t* __restrict__ sums,
+                                                                 uint32_t tiles,
+                                                                 uint32_t* __restrict__ total_out) {
+  __shared__ uint32_t ws[32];
+  uint32_t carry = 0;
+  for (uint32_t t0 = 0; t0 < tiles; t0 += kScanThreads) {
+    const uint32_t i = t0 + threadIdx.x;
+    const uint32_t v = (i < tiles) ? sums[i] : 0u;
+    uint32_t total;
+    const uint32_t ex = block_exclusive_scan(v, ws, &total);
+    if (i < tiles) sums[i] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) *total_out = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const uint32_t* __restrict__ in,
+                                                             uint64_t n,
+                                                             const uint32_t* __restrict__ tile_off,
+                                                             uint32_t* __restrict__ out) {
+  __shared__ uint32_t ws[32];
+  const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; i++) {
+    v[i] = (base + i < n) ? in[base + i] : 0u;
+    s += v[i];
+  }
+  uint32_t run = tile_off[blockIdx.x] + block_exclusive_scan(s, ws, nullptr);
+#pragma unroll
+  for (int i = 0; i < kScanItems; i++) {
+    if (base + i < n) out[base + i] = run;
+    run += v[i];
+  }
+}
+
+// Every kept edge b -> p becomes the entry b in p's CSR segment (order fixed later by sorting).
+__global__ void k_scatter_reverse(const uint32_t* __restrict__ pruned,
+                                  const uint32_t* __restrict__ pruned_num, uint32_t p_len,
+                                  uint64_t n, const uint32_t* __restrict__ offs,
+                                  uint32_t* __restrict__ cursor, uint32_t* __restrict__ edges) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t b = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; b < n;
+       b += stride) {
+    const uint32_t cnt = pruned_num[b];
+    for (uint32_t t = 0; t < cnt; t++) {
+      const uint32_t dst = pruned[b * p_len + t];
+      const uint32_t pos = atomicAdd(cursor + dst, 1u);
+      edges[offs[dst] + pos] = static_cast<uint32_t>(b);
+    }
+  }
+}
+
+// Reverse list of node p: the R smallest sources of its segment in ascending order, which is
+// what add_reverse (Gbuilder.cuh:1020-1038) stores when sources run in ascending order; the
+// count is min(in-degree, R).  Segments longer than 128 keep a running 128-smallest set.
+__global__ void __launch_bounds__(256) k_reverse_lists(const uint32_t* __restrict__ offs,
+                                                       const uint32_t* __restrict__ edges,
+                                                       uint64_t n, uint32_t r,
+                                                       uint32_t* __restrict__ rev,
+                                                       uint32_t* __restrict__ rev_num) {
+  const uint32_t lane = lane_id();
+  const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (blockDim.x >> 5);
+  for (uint64_t p = blockIdx.x * static_cast<uint64_t>(blockDim.x >> 5) + (threadIdx.x >> 5);
+       p < n; p += nwarps) {
+    const uint32_t o0 = offs[p];
+    const uint32_t deg = offs[p + 1] - o0;
+    const uint32_t cnt = min(deg, r);
+    if (deg == 0) {
+      if (lane == 0) rev_num[p] = 0;
+      continue;
+    }
+    uint32_t best[4];
+    for (uint32_t c0 = 0; c0 < deg; c0 += 128) {
+      uint32_t chunk[4];
+#pragma unroll
+      for (int s = 0; s < 4; s++) {
+        const uint32_t i = c0 + static_cast<uint32_t>(s) * 32u + lane;
+        chunk[s] = (i < deg) ? edges[o0 + i] : 0xFFFFFFFFu;
+      }
+      warp_sort_u32<4>(chunk);
+      if (c0 == 0) {
+#pragma unroll
+        for (int s = 0; s < 4; s++) best[s] = chunk[s];
+      } else {
+        // best (ascending) against chunk reversed: the element-wise minimum holds the 128
+        // smallest as a bitonic sequence, which one merge pass sorts.
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+          const uint32_t rv = __shfl_sync(kFull, chunk[3 - s], 31 - lane);
+          best[s] = min(best[s], rv);
+        }
+        warp_bitonic_merge_u32<4>(best);
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+      const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
+      if (i < cnt) rev[p * r + i] = best[s];
+    }
+    if (lane == 0) rev_num[p] = cnt;
+  }
+}
+
+// ------------------------------------------------------------------ K3: merge + prune
+// fusion_merge_sort_prune_kernel (Gbuilder.cuh:1467-1601): merged list = reverse entries then
+// pruned entries (pr_sort_list view); sort by distance keeping that order on ties; RNG prune
+// into the out row; non-strict fill with first-occurrence marking; tomb padding.
+template <int E>
+__global__ void __launch_bounds__(256) k_merge_prune(MergeArgs a) {
+  constexpr int C_MAX = 32 * E;
+  extern __shared__ uint32_t smem_u32[];
+  const uint32_t lane = lane_id();
+  const uint32_t warp = threadIdx.x >> 5;
+  uint32_t* ids_s = smem_u32 + warp * (3 * C_MAX + C_MAX / 4);
+  float* dist_s = reinterpret_cast<float*>(ids_s + C_MAX);
+  uint32_t* out_s = ids_s + 2 * C_MAX;
+  uint8_t* added_s = reinterpret_cast<uint8_t*>(ids_s + 3 * C_MAX);
+  const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (blockDim.x >> 5);
+  uint64_t ev = 0;
+  for (uint64_t b = blockIdx.x * static_cast<uint64_t>(blockDim.x >> 5) + warp; b < a.n;
+       b += nwarps) {
+    const uint32_t rn = min(a.reverse_num[b], a.r);
+    const uint32_t pn = a.pruned_num[b];
+    const uint32_t nn = rn + pn;
+    uint32_t* orow = a.out + b * a.degree;
+    if (nn == 0) {
+      for (uint32_t t = lane; t < a.degree; t += 32) orow[t] = kTomb;
+      continue;
+    }
+    uint32_t id[E];
+    bool valid[E];
+#pragma unroll
+    for (int s = 0; s < E; s++) {
+      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+      uint32_t x = kTomb;
+      if (j < rn)
+        x = a.reverse[b * a.r + j];
+      else if (j < nn)
+        x = a.pruned[b * a.p + (j - rn)];
+      if (j < nn && x >= a.n) {  // out-of-range input id
+        raise_error(a.status, kErrBadId);
+        x = kTomb;
+      }
+      id[s] = x;
+      valid[s] = j < nn && x != kTomb;
+    }
+    float dist[E];
+    dist_seq_multi<E>(a.base + b * a.d, a.base, a.d, id, valid, dist);
+    uint64_t key[E];
+#pragma unroll
+    for (int s = 0; s < E; s++) {
+      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+      key[s] = (j < nn) ? pack_key(dist[s], j) : ~0ull;
+    }
+    if (lane == 0) ev += nn;
+    warp_sort_kv<E>(key, id);
+#pragma unroll
+    for (int s = 0; s < E; s++) {
+      const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
+      if (i < nn) {
+        ids_s[i] = id[s];
+        dist_s[i] = key_dist(key[s]);
+      }
+    }
+    __syncwarp();
+    if (lane == 0) out_s[0] = ids_s[0];
+    __syncwarp();
+    uint32_t k = 0;
+    uint64_t checks = 0;
+    for (uint32_t j = 1; j < nn; j++) {
+      const uint32_t x = ids_s[j];
+      if (!occluded(a.base, a.n, a.d, x, dist_s[j], out_s, k, &checks)) {
+        k++;
+        if (lane == 0) out_s[k] = x;
+        __syncwarp();
+        if (k == a.degree - 1) break;
+      }
+    }
+    if (!a.strict && k < a.degree - 1) {
+      for (uint32_t i = lane; i < nn; i += 32) added_s[i] = 0;
+      __syncwarp();
+      for (uint32_t i = 0; i <= k; i++) {  // first occurrence of each kept id
+        const uint32_t x = out_s[i];
+        for (uint32_t j0 = 0; j0 < nn; j0 += 32) {
+          const uint32_t j = j0 + lane;
+          const unsigned m = __ballot_sync(kFull, j < nn && ids_s[j] == x);
+          if (m) {
+            if (lane == 0) added_s[j0 + __ffs(static_cast<int>(m)) - 1] = 1;
+            break;
+          }
+        }
+        __syncwarp();
+      }
+      for (uint32_t i = 0; i < nn && k < a.degree - 1; i++) {
+        if (added_s[i]) continue;
+        const uint32_t x = ids_s[i];
+        if (x != kTomb && x != static_cast<uint32_t>(b) && x < a.n) {
+          k++;
+          if (lane == 0) out_s[k] = x;
+          __syncwarp();
+        }
+      }
+    }
+    ev += (lane == 0) ? checks : 0;
+    for (uint32_t t = lane; t < a.degree; t += 32) orow[t] = (t <= k) ? out_s[t] : kTomb;
+    __syncwarp();
+  }
+  if (lane == 0 && ev) atomicAdd(a.evals, static_cast<unsigned long long>(ev));
+}
+
+// ------------------------------------------------------------------ launchers
+static int grid_for(uint64_t items, int per_block, int num_sms, int max_per_sm) {
+  uint64_t blocks = (items + per_block - 1) / per_block;
+  uint64_t cap = static_cast<uint64_t>(num_sms) * max_per_sm;
+  if (blocks > cap) blocks = cap;
+  if (blocks == 0) blocks = 1;
+  return static_cast<int>(blocks);
+}
+
+cudaError_t launch_match_winner(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint64_t n,
+                                uint32_t* winner, uint32_t* status, int num_sms,
+                                cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(winner, 0xFF, n * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  k_match_winner<<<grid_for(q, 256, num_sms, 8), 256, 0, st>>>(gt, q, gt_k, n, winner, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_match_rows(const uint32_t* gt, uint32_t gt_k, uint64_t n,
+                              const uint32_t* winner, uint32_t* out, int num_sms,
+                              cudaStream_t st) {
+  k_match_rows<<<grid_for(n * gt_k, 256, num_sms, 8), 256, 0, st>>>(gt, gt_k, n, winner, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_validate_ids(const uint32_t* ids, uint64_t count, uint64_t n,
+                                uint32_t* status, int num_sms, cudaStream_t st) {
+  k_validate_ids<<<grid_for(count, 256, num_sms, 8), 256, 0, st>>>(ids, count, n, status);
+  return cudaGetLastError();
+}
+
+template <int E, bool P1>
+static cudaError_t launch_prune_e(const PruneArgs& a, int num_sms, cudaStream_t st) {
+  const int threads = 256;
+  const size_t smem = (threads / 32) * 3 * 32 * E * sizeof(uint32_t);
+  k_prune_reverse<E, P1><<<grid_for(a.n, threads / 32, num_sms, 8), threads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prune_reverse(const PruneArgs& a, bool phase1, int num_sms, cudaStream_t st) {
+  if (a.c <= 32) return phase1 ? launch_prune_e<1, true>(a, num_sms, st)
+                               : launch_prune_e<1, false>(a, num_sms, st);
+  if (a.c <= 64) return phase1 ? launch_prune_e<2, true>(a, num_sms, st)
+                               : launch_prune_e<2, false>(a, num_sms, st);
+  return phase1 ? launch_prune_e<4, true>(a, num_sms, st)
+                : launch_prune_e<4, false>(a, num_sms, st);
+}
+
+cudaError_t launch_reverse_csr(const uint32_t* pruned, const uint32_t* pruned_num, uint32_t p_len,
+                               uint64_t n, const uint32_t* indeg, uint32_t* offs,
+                               uint32_t* tile_sums, uint32_t* cursor, uint32_t* edges,
+                               int num_sms, cudaStream_t st) {
+  const uint32_t tiles = static_cast<uint32_t>((n + kScanTile - 1) / kScanTile);
+  k_scan_tiles<<<tiles, kScanThreads, 0, st>>>(indeg, n, tile_sums);
+  k_scan_tile_sums<<<1, kScanThreads, 0, st>>>(tile_sums, tiles, offs + n);
+  k_scan_apply<<<tiles, kScanThreads, 0, st>>>(indeg, n, tile_sums, offs);
+  cudaError_t e = cudaMemsetAsync(cursor, 0, n * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  k_scatter_reverse<<<grid_for(n, 256, num_sms, 8), 256, 0, st>>>(pruned, pruned_num, p_len, n,
+                                                                   offs, cursor, edges);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reverse_lists(const uint32_t* offs, const uint32_t* edges, uint64_t n,
+                                 uint32_t r, uint32_t* rev, uint32_t* rev_num, int num_sms,
+                                 cudaStream_t st) {
+  k_reverse_lists<<<grid_for(n, 8, num_sms, 8), 256, 0, st>>>(offs, edges, n, r, rev, rev_num);
+  return cudaGetLastError();
+}
+
+template <int E>
+static cudaError_t launch_merge_e(const MergeArgs& a, int num_sms, cudaStream_t st) {
+  const int threads = 256;
+  const size_t smem = (threads / 32) * (3 * 32 * E + 8 * E) * sizeof(uint32_t);
+  k_merge_prune<E><<<grid_for(a.n, threads / 32, num_sms, 8), threads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_merge_prune(const MergeArgs& a, int num_sms, cudaStream_t st) {
+  const uint32_t cmax = a.r + a.p;
+  if (cmax <= 32) return launch_merge_e<1>(a, num_sms, st);
+  if (cmax <= 64) return launch_merge_e<2>(a, num_sms, st);
+  return launch_merge_e<4>(a, num_sms, st);
+}
+
+}  // namespace pg

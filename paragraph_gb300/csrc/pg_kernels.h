@@ -1,0 +1,85 @@
+// pg_kernels.h -- kernel argument blocks and launchers (host-visible, no device code).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pg {
+
+struct PruneArgs {
+  const float* base;
+  uint64_t n;
+  uint32_t d;
+  const uint32_t* graph;   // n x c candidate rows (link rounds)
+  uint32_t c;              // candidates per node
+  const uint32_t* gt;      // phase 1: ground truth q x gt_k
+  const uint32_t* winner;  // phase 1: winner key per base
+  uint32_t gt_k;
+  uint32_t p;              // pruned list length
+  int strict;
+  uint32_t* pruned;        // n x p
+  uint32_t* pruned_num;    // n
+  uint32_t* indeg;         // n, incremented per kept edge (reverse in-degree)
+  uint32_t* sorted;        // optional n x c: candidate rows after the sort
+  unsigned long long* evals;
+  uint32_t* status;        // error flags (kErr*)
+};
+
+struct MergeArgs {
+  const float* base;
+  uint64_t n;
+  uint32_t d;
+  const uint32_t* pruned;
+  const uint32_t* pruned_num;
+  uint32_t p;
+  const uint32_t* reverse;
+  const uint32_t* reverse_num;
+  uint32_t r;
+  uint32_t degree;
+  int strict;
+  uint32_t* out;  // n x degree
+  unsigned long long* evals;
+  uint32_t* status;
+};
+
+struct SearchArgs {
+  const float* base;
+  uint64_t n;
+  uint32_t d;
+  const uint32_t* graph;  // n x graph_degree
+  uint32_t graph_degree;
+  uint32_t km, kp, kd, reset_iter, seed_base;
+  uint32_t max_iters;
+  const uint32_t* order;  // optional query order (permutation of 0..n-1), NULL = identity
+  uint32_t* out;          // n x (km + kp*kd)
+  unsigned long long* evals;
+  unsigned long long* iters;
+  uint32_t* work;         // work counter, zeroed before the launch
+  uint32_t* status;
+  uint32_t hash_slots;    // visited-set capacity per warp (power of two)
+};
+
+cudaError_t launch_match_winner(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint64_t n,
+                                uint32_t* winner, uint32_t* status, int num_sms, cudaStream_t st);
+cudaError_t launch_match_rows(const uint32_t* gt, uint32_t gt_k, uint64_t n,
+                              const uint32_t* winner, uint32_t* out, int num_sms,
+                              cudaStream_t st);
+cudaError_t launch_validate_ids(const uint32_t* ids, uint64_t count, uint64_t n,
+                                uint32_t* status, int num_sms, cudaStream_t st);
+cudaError_t launch_prune_reverse(const PruneArgs& a, bool phase1, int num_sms, cudaStream_t st);
+cudaError_t launch_reverse_csr(const uint32_t* pruned, const uint32_t* pruned_num, uint32_t p_len,
+                               uint64_t n, const uint32_t* indeg, uint32_t* offs,
+                               uint32_t* tile_sums, uint32_t* cursor, uint32_t* edges,
+                               int num_sms, cudaStream_t st);
+cudaError_t launch_reverse_lists(const uint32_t* offs, const uint32_t* edges, uint64_t n,
+                                 uint32_t r, uint32_t* rev, uint32_t* rev_num, int num_sms,
+                                 cudaStream_t st);
+cudaError_t launch_merge_prune(const MergeArgs& a, int num_sms, cudaStream_t st);
+// Returns cudaErrorInvalidValue for parameter combinations the search kernel was not built for
+// (see search_supported).
+cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, cudaStream_t st);
+bool search_supported(uint32_t d, uint32_t km, uint32_t kp, uint32_t kd);
+size_t search_smem_per_warp(uint32_t d, uint32_t hash_slots);
+
+constexpr uint32_t kScanTileElems = 4096;
+
+}  // namespace pg

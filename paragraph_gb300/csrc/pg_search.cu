@@ -1,0 +1,383 @@
+// pg_search.cu -- beam search with every base point as the query (K4/K8).
+//
+// Semantics of link_process_v0_store_base_data (Gsearcher.cuh:890-1066): list of L = Km + Kp*Kd
+// (distance, id); seeds (seed_base + i) % n in slots Km.., Km slots at FLT_MAX; sort; visited set
+// = the top Km; loop { pick the first Kp unexplored of the top Km (collect_top_p_normal,
+// Gsearcher.cuh:75-106) and mark them; read their first Kd graph neighbours; score each new id
+// (visited or repeated ids get FLT_MAX); sort; every reset_iter iterations rebuild the visited set
+// from the top Km }.  Output: all L ids with the parent bit cleared.
+//
+// GB300 design, one warp per query, persistent warps pulling queries from a work counter:
+//   * the list lives in registers (32*E slots, element i = lane i%32, slot i/32) and is sorted with
+//     a warp bitonic network on (distance, position) keys = the stable order of the reference;
+//   * the visited set is an exact open-addressing table in shared memory (Ghashtable semantics);
+//   * the candidate rows of one iteration are staged into shared memory with one cp.async.bulk
+//     per new candidate (16-byte aligned 4*D-byte rows) completing on an mbarrier;
+//   * distances keep the reference's FP32 order exactly: residue r = i mod 32 accumulates
+//     q[i]*x[i] in i order, then the shuffle-down tree 16,8,4,2,1.  Eight lanes cover one row
+//     (lane m owns residues 4m..4m+3 via 128-bit shared loads), four rows per pass, and a
+//     transposed butterfly (xor 4, 2, 1 + two in-register adds) forms exactly that tree.
+#include "pg_device.cuh"
+#include "pg_kernels.h"
+
+namespace pg {
+
+namespace {
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_addr(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false if the phase did not complete within the limit.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t t = 0; t < (1u << 22); t++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void bulk_row_to_smem(float* dst, const float* src, uint32_t bytes,
+                                                 uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t hslot(uint32_t key, uint32_t mask) {
+  uint32_t h = key * 0x9E3779B1u;
+  h ^= h >> 16;
+  return h & mask;
+}
+
+__device__ __forceinline__ bool hash_contains(const uint32_t* t, uint32_t mask, uint32_t key) {
+  uint32_t s = hslot(key, mask);
+  for (uint32_t probe = 0; probe <= mask; probe++) {
+    const uint32_t v = t[s];
+    if (v == 0) return false;
+    if (v == key + 1) return true;
+    s = (s + 1) & mask;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void hash_insert(uint32_t* t, uint32_t mask, uint32_t key) {
+  uint32_t s = hslot(key, mask);
+  for (uint32_t probe = 0; probe <= mask; probe++) {
+    const uint32_t old = atomicCAS(t + s, 0u, key + 1);
+    if (old == 0 || old == key + 1) return;
+    s = (s + 1) & mask;
+  }
+}
+
+__device__ __forceinline__ void hash_clear(uint32_t* t, uint32_t slots) {
+  uint4* t4 = reinterpret_cast<uint4*>(t);
+  for (uint32_t i = lane_id(); i < (slots >> 2); i += 32) t4[i] = make_uint4(0, 0, 0, 0);
+}
+
+template <int NS>
+struct Q4 {
+  float4 v[NS];
+};
+
+// Stage the rows of this warp's new candidates into shared memory and return this lane's
+// distance (FLT_MAX where newc is false).  Returns false in *ok when the bounded wait failed.
+template <int KSTEPS>
+__device__ __forceinline__ float stage_and_score(const SearchArgs& a, const Q4<KSTEPS>& q,
+                                                 uint32_t node, bool newc, float* rows,
+                                                 uint64_t* mbar, uint32_t& phase, bool& ok) {
+  const uint32_t lane = lane_id();
+  const unsigned newmask = __ballot_sync(kFull, newc);
+  const uint32_t nnew = __popc(newmask);
+  if (nnew == 0) return FLT_MAX;
+  const uint32_t d = a.d;
+  const uint32_t ci = __popc(newmask & ((1u << lane) - 1u));  // compact slot of this lane
+  fence_proxy_async();
+  if (lane == 0) mbar_arrive_expect_tx(mbar, nnew * d * 4u);
+  __syncwarp();
+  if (newc)
+    bulk_row_to_smem(rows + static_cast<size_t>(ci) * d, a.base + static_cast<uint64_t>(node) * d,
+                     d * 4u, mbar);
+  ok = mbar_wait_bounded(mbar, phase);
+  phase ^= 1u;
+  if (!ok) return FLT_MAX;
+
+  const uint32_t g = lane >> 3, m = lane & 7u;
+  float p[8][4];
+#pragma unroll
+  for (int r = 0; r < 8; r++)
+#pragma unroll
+    for (int i = 0; i < 4; i++) p[r][i] = 0.0f;
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    if (4u * r < nnew) {
+      const uint32_t c = 4u * r + g;
+      if (c < nnew) {
+        const float* row = rows + static_cast<size_t>(c) * d;
+#pragma unroll
+        for (int k = 0; k < KSTEPS; k++) {
+          const uint32_t off = 32u * k + 4u * m;
+          if (off < d) {
+            const float4 x = *reinterpret_cast<const float4*>(row + off);
+            p[r][0] = fmaf(q.v[k].x, x.x, p[r][0]);
+            p[r][1] = fmaf(q.v[k].y, x.y, p[r][1]);
+            p[r][2] = fmaf(q.v[k].z, x.z, p[r][2]);
+            p[r][3] = fmaf(q.v[k].w, x.w, p[r][3]);
+          }
+        }
+      }
+    }
+  }
+  // transposed shuffle tree: xor 4 (residues +16), xor 2 (+8), xor 1 (+4)
+  const bool bA = (m & 4u) != 0, bB = (m & 2u) != 0, bC = (m & 1u) != 0;
+  float a4[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const float send = bA ? p[i][j] : p[i + 4][j];
+      const float keep = bA ? p[i + 4][j] : p[i][j];
+      a4[i][j] = keep + __shfl_xor_sync(kFull, send, 4);
+    }
+  float b2[2][4];
+#pragma unroll
+  for (int i = 0; i < 2; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const float send = bB ? a4[i][j] : a4[i + 2][j];
+      const float keep = bB ? a4[i + 2][j] : a4[i][j];
+      b2[i][j] = keep + __shfl_xor_sync(kFull, send, 2);
+    }
+  float v[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const float send = bC ? b2[0][j] : b2[1][j];
+    const float keep = bC ? b2[1][j] : b2[0][j];
+    v[j] = keep + __shfl_xor_sync(kFull, send, 1);
+  }
+  const float total = (v[0] + v[2]) + (v[1] + v[3]);  // levels 2 and 1 of the tree
+  // lane (g, m) holds candidate 4m + g; route it to the lane that owns that candidate
+  const uint32_t src = newc ? (((ci & 3u) << 3) | (ci >> 2)) : 0u;
+  const float dist = -__shfl_sync(kFull, total, src);
+  return newc ? dist : FLT_MAX;
+}
+
+}  // namespace
+
+template <int KM_S, int KSTEPS>
+__global__ void __launch_bounds__(32) k_search(SearchArgs a) {
+  constexpr int E = (KM_S + 1 <= 2) ? 2 : 4;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const uint32_t lane = lane_id();
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw);
+  uint32_t* hash = reinterpret_cast<uint32_t*>(smem_raw + 16);
+  float* rows = reinterpret_cast<float*>(smem_raw + 16 + 4u * a.hash_slots);
+  const uint32_t hmask = a.hash_slots - 1u;
+  const uint32_t km = a.km, kp = a.kp, kd = a.kd;
+  const uint32_t L = km + 32u;
+  if (lane == 0) mbar_init(mbar, 1);
+  __syncwarp();
+  uint32_t phase = 0;
+  unsigned long long ev = 0, it_all = 0;
+  bool ok = true;
+  const uint32_t g = lane >> 3, m = lane & 7u;
+  const uint32_t e_of_lane = lane / kd, nb_of_lane = lane % kd;
+
+  for (;;) {
+    uint32_t qi = 0;
+    if (lane == 0) qi = atomicAdd(a.work, 1u);
+    qi = __shfl_sync(kFull, qi, 0);
+    if (qi >= a.n) break;
+    const uint32_t qid = a.order ? a.order[qi] : qi;
+    const float* qrow = a.base + static_cast<uint64_t>(qid) * a.d;
+    Q4<KSTEPS> q;
+#pragma unroll
+    for (int k = 0; k < KSTEPS; k++) {
+      const uint32_t off = 32u * k + 4u * m;
+      q.v[k] = (off < a.d) ? __ldg(reinterpret_cast<const float4*>(qrow + off))
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    (void)g;
+    uint64_t key[E];
+    uint32_t id[E];
+#pragma unroll
+    for (int s = 0; s < E; s++) {
+      key[s] = ~0ull;
+      id[s] = kTomb;
+    }
+#pragma unroll
+    for (int s = 0; s < KM_S; s++) key[s] = pack_key(FLT_MAX, static_cast<uint32_t>(s) * 32u + lane);
+
+    // seeds: every slot is scored (Gsearcher.cuh:958-976 has no visited test)
+    {
+      const uint32_t node = static_cast<uint32_t>((a.seed_base + static_cast<uint64_t>(lane)) % a.n);
+      const float dist = stage_and_score<KSTEPS>(a, q, node, true, rows, mbar, phase, ok);
+      if (!ok) break;
+      key[KM_S] = pack_key(dist, km + lane);
+      id[KM_S] = node;
+      ev += (lane == 0) ? 32u : 0u;
+    }
+    warp_sort_kv<E>(key, id);
+    hash_clear(hash, a.hash_slots);
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < KM_S; s++) hash_insert(hash, hmask, id[s] & kMaskedTomb);
+    __syncwarp();
+
+    uint32_t iter = 0, total = 0;
+    for (;;) {
+      // collect_top_p_normal: first kp unexplored of the top km, mark them explored
+      uint32_t found = 0;
+      uint32_t ex_lane = kTomb;  // lane e holds explore id e
+#pragma unroll
+      for (int s = 0; s < KM_S; s++) {
+        if (found < kp) {
+          const bool unexp = (id[s] & kParent) == 0;
+          const unsigned mask = __ballot_sync(kFull, unexp);
+          const uint32_t cnt = __popc(mask);
+          const uint32_t rank = __popc(mask & ((1u << lane) - 1u));
+          const bool want = lane >= found && lane < found + cnt && lane < kp;
+          const uint32_t src = want ? __fns(mask, 0, static_cast<int>(lane - found + 1)) : 0u;
+          const uint32_t got = __shfl_sync(kFull, id[s], src);
+          if (want) ex_lane = got;
+          if (unexp && found + rank < kp) id[s] |= kParent;
+          found += cnt;
+        }
+      }
+      if (found == 0) break;
+      if (++total > a.max_iters) {
+        if (lane == 0) raise_error(a.status, kErrIterCap);
+        break;
+      }
+      const uint32_t ex = __shfl_sync(kFull, ex_lane, e_of_lane);
+      uint32_t node =
+          (ex != kTomb) ? a.graph[static_cast<uint64_t>(ex) * a.graph_degree + nb_of_lane] : kTomb;
+      if (node >= a.n && node != kTomb) {  // out-of-range graph entry
+        raise_error(a.status, kErrBadId);
+        node = kTomb;
+      }
+      const bool valid = node != kTomb;
+      const unsigned same = __match_any_sync(kFull, node);
+      const bool first = lane == static_cast<uint32_t>(__ffs(static_cast<int>(same)) - 1);
+      const bool newc = valid && first && !hash_contains(hash, hmask, node);
+      __syncwarp();
+      if (newc) hash_insert(hash, hmask, node);
+      __syncwarp();
+      const float dist = stage_and_score<KSTEPS>(a, q, node, newc, rows, mbar, phase, ok);
+      if (!ok) break;
+      ev += (lane == 0) ? __popc(__ballot_sync(kFull, newc)) : 0u;
+#pragma unroll
+      for (int s = 0; s < KM_S; s++)
+        key[s] = (key[s] & 0xFFFFFFFF00000000ull) | (static_cast<uint32_t>(s) * 32u + lane);
+      key[KM_S] = pack_key(dist, km + lane);
+      id[KM_S] = node;
+#pragma unroll
+      for (int s = KM_S + 1; s < E; s++) {
+        key[s] = ~0ull;
+        id[s] = kTomb;
+      }
+      warp_sort_kv<E>(key, id);
+      if (++iter == a.reset_iter) {
+        hash_clear(hash, a.hash_slots);
+        __syncwarp();
+#pragma unroll
+        for (int s = 0; s < KM_S; s++) hash_insert(hash, hmask, id[s] & kMaskedTomb);
+        __syncwarp();
+        iter = 0;
+      }
+    }
+    if (!ok) break;
+    it_all += (lane == 0) ? total : 0u;
+    uint32_t* orow = a.out + static_cast<uint64_t>(qid) * L;
+#pragma unroll
+    for (int s = 0; s < E; s++) {
+      const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
+      if (i < L) orow[i] = id[s] & kMaskedTomb;
+    }
+  }
+  if (!ok) {
+    if (lane == 0) raise_error(a.status, kErrWait);
+    mbar_wait_bounded(mbar, phase ^ 1u);  // let a late copy land before the block exits
+  }
+  if (lane == 0) {
+    if (ev) atomicAdd(a.evals, ev);
+    if (it_all) atomicAdd(a.iters, it_all);
+  }
+}
+
+bool search_supported(uint32_t d, uint32_t km, uint32_t kp, uint32_t kd) {
+  return d > 0 && d <= 512 && (d % 4) == 0 && kp * kd == 32 && kp >= 1 && km >= 32 &&
+         km <= 96 && (km % 32) == 0;
+}
+
+size_t search_smem_per_warp(uint32_t d, uint32_t hash_slots) {
+  return 16 + 4 * static_cast<size_t>(hash_slots) + 32 * 4 * static_cast<size_t>(d);
+}
+
+template <int KM_S, int KS>
+static cudaError_t launch_search_t(const SearchArgs& a, int num_sms, size_t smem_optin,
+                                   cudaStream_t st) {
+  const size_t smem = search_smem_per_warp(a.d, a.hash_slots);
+  if (smem > smem_optin) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_search<KM_S, KS>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<KM_S, KS>, 32, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  uint64_t blocks = static_cast<uint64_t>(num_sms) * per_sm;
+  if (blocks > a.n) blocks = a.n;
+  k_search<KM_S, KS><<<static_cast<unsigned>(blocks), 32, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, cudaStream_t st) {
+  if (!search_supported(a.d, a.km, a.kp, a.kd)) return cudaErrorInvalidValue;
+  const int km_s = static_cast<int>(a.km / 32);
+  const bool small = a.d <= 256;
+  switch (km_s) {
+    case 1:
+      return small ? launch_search_t<1, 8>(a, num_sms, smem_optin, st)
+                   : launch_search_t<1, 16>(a, num_sms, smem_optin, st);
+    case 2:
+      return small ? launch_search_t<2, 8>(a, num_sms, smem_optin, st)
+                   : launch_search_t<2, 16>(a, num_sms, smem_optin, st);
+    default:
+      return small ? launch_search_t<3, 8>(a, num_sms, smem_optin, st)
+                   : launch_search_t<3, 16>(a, num_sms, smem_optin, st);
+  }
+}
+
+}  // namespace pg
