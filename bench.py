@@ -333,7 +333,8 @@ def run_ours(args):
                                        f"M={args.degree}, L={args.beam}",
                            "n": args.n, "d": args.d, "q": args.n, "degree": args.degree,
                            "beam": args.beam, "parallelism": "replicas" if world > 1 else "single",
-                           "l2": "inputs larger than L2 (base 800 MB, gt 512 MB)",
+                           "l2": f"inputs larger than L2 (base {n * d * 4 / 1e6:.0f} MB, "
+                                 f"gt {n * 128 * 4 / 1e6:.0f} MB vs 129 MB L2)",
                            "build_s": round(ms_step / 1e3, 4)},
                 "evals_per_build": evals,
                 "stage_ms": {"proj": round(s.ms_proj, 2),

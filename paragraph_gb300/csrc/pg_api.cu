@@ -194,9 +194,9 @@ int check_params(const pg_params* p, uint64_t n, uint32_t d, uint64_t q) {
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 int status_to_error(uint32_t s) {
-  if (s & 4u) return fail(PG_EINVAL, "input holds an id >= n that is not tomb");
-  if (s & 1u) return fail(PG_ETIMEOUT, "a search exceeded max_search_iters");
-  if (s & 2u) return fail(PG_ETIMEOUT, "a bounded device wait gave up");
+  if (s & 4u) return fail(PG_EINVAL, "input holds an id >= n that is not tomb (status 0x%x)", s);
+  if (s & 1u) return fail(PG_ETIMEOUT, "a search exceeded max_search_iters (status 0x%x)", s);
+  if (s & 2u) return fail(PG_ETIMEOUT, "a bounded device wait gave up (status 0x%x)", s);
   if (s) return fail(PG_ECUDA, "device status 0x%x", s);
   return PG_OK;
 }

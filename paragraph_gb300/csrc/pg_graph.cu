@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(256) k_merge_prune(MergeArgs a) {
   for (uint64_t b = blockIdx.x * static_cast<uint64_t>(blockDim.x >> 5) + warp; b < a.n;
        b += nwarps) {
     const uint32_t rn = min(a.reverse_num[b], a.r);
-    const uint32_t pn = a.pruned_num[b];
+    const uint32_t pn = min(a.pruned_num[b], a.p);
     const uint32_t nn = rn + pn;
     uint32_t* orow = a.out + b * a.degree;
     if (nn == 0) {

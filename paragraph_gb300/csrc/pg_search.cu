@@ -54,11 +54,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: false if the phase did not complete within the limit.
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: false if the phase did not complete within one second of wall time.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t t = 0; t < (1u << 22); t++)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (global_ns() - t0 > 1000000000ull) return false;
+  return true;
 }
 
 __device__ __forceinline__ void bulk_row_to_smem(float* dst, const float* src, uint32_t bytes,
@@ -267,7 +275,12 @@ __global__ void __launch_bounds__(32) k_search(SearchArgs a) {
           const uint32_t cnt = __popc(mask);
           const uint32_t rank = __popc(mask & ((1u << lane) - 1u));
           const bool want = lane >= found && lane < found + cnt && lane < kp;
-          const uint32_t src = want ? __fns(mask, 0, static_cast<int>(lane - found + 1)) : 0u;
+          uint32_t src = 0;
+          if (want) {  // position of set bit number (lane - found) of mask
+            unsigned mm = mask;
+            for (uint32_t i = found; i < lane; i++) mm &= mm - 1u;
+            src = static_cast<uint32_t>(__ffs(static_cast<int>(mm)) - 1);
+          }
           const uint32_t got = __shfl_sync(kFull, id[s], src);
           if (want) ex_lane = got;
           if (unexp && found + rank < kp) id[s] |= kParent;
@@ -280,8 +293,11 @@ __global__ void __launch_bounds__(32) k_search(SearchArgs a) {
         break;
       }
       const uint32_t ex = __shfl_sync(kFull, ex_lane, e_of_lane);
-      uint32_t node =
-          (ex != kTomb) ? a.graph[static_cast<uint64_t>(ex) * a.graph_degree + nb_of_lane] : kTomb;
+      uint32_t node = kTomb;
+      if (ex < a.n)
+        node = a.graph[static_cast<uint64_t>(ex) * a.graph_degree + nb_of_lane];
+      else if (ex != kTomb)
+        raise_error(a.status, kErrCapacity);  // not reachable: list ids are < n or tomb
       if (node >= a.n && node != kTomb) {  // out-of-range graph entry
         raise_error(a.status, kErrBadId);
         node = kTomb;
@@ -295,7 +311,8 @@ __global__ void __launch_bounds__(32) k_search(SearchArgs a) {
       __syncwarp();
       const float dist = stage_and_score<KSTEPS>(a, q, node, newc, rows, mbar, phase, ok);
       if (!ok) break;
-      ev += (lane == 0) ? __popc(__ballot_sync(kFull, newc)) : 0u;
+      const unsigned scored = __ballot_sync(kFull, newc);  // every lane takes part
+      ev += (lane == 0) ? __popc(scored) : 0u;
 #pragma unroll
       for (int s = 0; s < KM_S; s++)
         key[s] = (key[s] & 0xFFFFFFFF00000000ull) | (static_cast<uint32_t>(s) * 32u + lane);
