@@ -87,9 +87,9 @@ def make_dataset_cuda(n: int, d: int, q: int | None = None, gt_k: int = 128, cen
     cent = torch.randn((centers, d), generator=gen, device=device, dtype=f32)
     comp = torch.randint(0, centers, (n,), generator=gen, device=device)
     base = cent[comp] + sigma * torch.randn((n, d), generator=gen, device=device, dtype=f32)
-    a = torch.randn((d, d), generator=gen, device=device, dtype=torch.float64)
-    qm, r = torch.linalg.qr(a)
-    rot = (qm * torch.sign(torch.diagonal(r))[None, :]).to(f32)
+    # the D x D rotation is built on the host (numpy QR): small, and independent of the GPU's
+    # linear-algebra libraries
+    rot = torch.from_numpy(_haar(np.random.Generator(np.random.PCG64(seed + 1)), d)).to(device)
     g = torch.randn((d,), generator=gen, device=device, dtype=f32)
     g = g * (shift_norm / g.norm())
     qcomp = torch.randint(0, centers, (q,), generator=gen, device=device)

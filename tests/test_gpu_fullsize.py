@@ -1,0 +1,55 @@
+"""Full-size parity: the 1M x 200 inner-product build (M=32, L=64) against the oracle.
+
+The oracle builds the same 1M-point graph on the host cores in seconds, so the benchmark's own
+workload is checked id for id (projection, final graph, evaluation counts), and two GPU builds
+must agree exactly (no run-to-run variation: every race of the reference has a canonical
+resolution here).
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+N, D = 1_000_000, 200
+
+
+@pytest.fixture(scope="module")
+def workload():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from paragraph_gb300 import datagen
+    base, gt = datagen.make_dataset_cuda(N, D, gt_k=128, seed=1234, device="cuda")
+    torch.cuda.synchronize()
+    return base, gt
+
+
+def test_full_size_build_matches_oracle(workload):
+    import paragraph_gb300 as pg
+    base, gt = workload
+    params = pg.default_params(32, 64)
+    graph = torch.empty((N, 32), dtype=torch.int32, device="cuda")
+    proj = torch.empty((N, 16), dtype=torch.int32, device="cuda")
+    with pg.Handle(0) as h:
+        st = h.build_device(base, gt, graph, proj, params)
+        g1 = graph.cpu().numpy().view(np.uint32).copy()
+        p1 = proj.cpu().numpy().view(np.uint32).copy()
+        st2 = h.build_device(base, gt, graph, proj, params)
+        g2 = graph.cpu().numpy().view(np.uint32)
+    assert np.array_equal(g1, g2), "two GPU builds differ"
+    assert st.evals_total == st2.evals_total
+    base_np = base.cpu().numpy()
+    gt_np = gt.cpu().numpy().view(np.uint32)
+    ref = oracle.build_graph(base_np, gt_np, degree=32, beam=64)
+    assert np.array_equal(p1, ref["proj"]), f"{(p1 != ref['proj']).any(axis=1).sum()} proj rows differ"
+    bad = (g1 != ref["graph"]).any(axis=1)
+    assert not bad.any(), f"{bad.sum()} of {N} graph rows differ"
+    assert st.evals_total == ref["stats"]["evals_total"]
+    assert list(st.search_iters)[:2] == ref["stats"]["iters_search"][:2]
+    # structural properties of the index
+    valid = g1 != pg.TOMB
+    assert (g1[valid] < N).all()
+    assert not (g1 == np.arange(N, dtype=np.uint32)[:, None]).any()
+    assert valid.sum(axis=1).max() <= 32
