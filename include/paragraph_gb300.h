@@ -149,6 +149,22 @@ int pg_search(pg_handle h, const float* d_base, uint64_t n, uint32_t d, const ui
               uint32_t seed_base, uint32_t max_iters, uint32_t* d_out, uint64_t* evals,
               uint64_t* iters);
 
+/* Same computation as pg_prune_reverse, for callers that cannot allocate device memory: a host
+ * application that owns the GPU through its own memory pool and forbids plugins to allocate, or
+ * a latency-bound caller that cannot take cudaMalloc's possible device-wide synchronisation.
+ * Needs no handle and allocates nothing: the reverse-edge workspace and counters live in a fixed
+ * array inside the library's device image (about 4.6 MB, held by every GPU that loads the
+ * library until the process exits).  Limits: n <= 32768 and n * pruned <= 1048576, else
+ * PG_EINVAL.  Runs on `stream` (a cudaStream_t) and synchronises it before returning.  All calls
+ * share the array: calls that overlap on the GPU race and must be serialised by the caller.  The
+ * first call on a device looks up the array's device address; make it before any stream capture.
+ * This entry point has no counterpart in the reference. */
+int pg_prune_reverse_noalloc(void* stream, const float* d_base, uint64_t n, uint32_t d,
+                             const uint32_t* d_graph, uint32_t c, uint32_t pruned,
+                             uint32_t reverse, int strict, uint32_t* d_pruned,
+                             uint32_t* d_pruned_num, uint32_t* d_reverse, uint32_t* d_reverse_num,
+                             uint64_t* evals);
+
 /* ---- on-disk formats ----------------------------------------------------------------------- */
 /* Raw vectors as read by read_vec_from_file (include/utils.hpp:17-35): headerless, exactly
  * count*elem_size bytes, or with the Big-ANN [u32 n][u32 d] header (README.md:13-21) when

@@ -95,6 +95,8 @@ SIGNATURES = {
                                       ctypes.c_int, _VP, _U64P]),
     "pg_search": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _U32, _U32, _U32, _U32, _U32, _U32,
                                  _U32, _VP, _U64P, _U64P]),
+    "pg_prune_reverse_noalloc": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _U32, _U32, _U32,
+                                                ctypes.c_int, _VP, _VP, _VP, _VP, _U64P]),
     "pg_read_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _VP, _U64, _U32P, _U32P]),
     "pg_save_graph": (ctypes.c_int, [ctypes.c_char_p, _VP, _U64, _U32, _U32]),
     "pg_entry_point": (ctypes.c_int, [_VP, _U64, _U32, _U64, _U32P]),

@@ -99,6 +99,8 @@ Layout make_layout(uint64_t n, uint32_t pmax, uint32_t rmax, uint32_t L, uint32_
 
 }  // namespace
 
+int pg::set_last_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 struct pg_handle_s {
   int device = 0;
   cudaStream_t stream = nullptr;

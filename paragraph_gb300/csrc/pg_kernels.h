@@ -82,4 +82,7 @@ size_t search_smem_per_warp(uint32_t d, uint32_t hash_slots);
 
 constexpr uint32_t kScanTileElems = 4096;
 
+// Records `msg` as the calling thread's pg_last_error() text and returns `code`.
+int set_last_error(int code, const char* msg);
+
 }  // namespace pg
