@@ -352,6 +352,328 @@ __global__ void __launch_bounds__(32) k_search(SearchArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Km = 32 path (one retained entry per lane).  Differences from k_search above:
+//   * candidate rows are staged ROWS at a time (ROWS*D*4 bytes of shared memory instead of 32
+//     rows), so several times more warps stay resident;
+//   * the sorted top 32 is kept in registers and the new candidates are merged into it by rank
+//     (ballot/popc against unique (distance, position) keys) -- the same total order as sorting
+//     the whole list, without the 64-key network every iteration;
+//   * the full 64-entry list (top before the last merge + the last candidates) is sorted once,
+//     when the query ends, for the output.
+namespace {
+
+// Scores the lanes whose `newc` is set, ROWS rows per pass (see stage_and_score for the FP32
+// order).  ROUNDS = ROWS/4 candidates per 8-lane group; the first log2(ROUNDS) butterfly levels
+// are transposed (each lane keeps one candidate), the remaining ones are plain xor reductions.
+template <int KSTEPS, int ROWS>
+__device__ __forceinline__ float score_passes(const SearchArgs& a, const Q4<KSTEPS>& q,
+                                              uint32_t node, bool newc, float* rows,
+                                              uint64_t* mbar, uint32_t& phase, bool& ok) {
+  constexpr int ROUNDS = ROWS / 4;
+  static_assert(ROUNDS == 2 || ROUNDS == 4 || ROUNDS == 8, "ROWS must be 8, 16 or 32");
+  const uint32_t lane = lane_id();
+  const unsigned newmask = __ballot_sync(kFull, newc);
+  const uint32_t nnew = __popc(newmask);
+  const uint32_t d = a.d;
+  const uint32_t ci = __popc(newmask & ((1u << lane) - 1u));
+  const uint32_t g = lane >> 3, m = lane & 7u;
+  const bool bA = (m & 4u) != 0, bB = (m & 2u) != 0, bC = (m & 1u) != 0;
+  float result = FLT_MAX;
+  for (uint32_t c0 = 0; c0 < nnew; c0 += ROWS) {
+    const uint32_t cnt = min(static_cast<uint32_t>(ROWS), nnew - c0);
+    const bool mine = newc && ci >= c0 && ci < c0 + ROWS;
+    fence_proxy_async();
+    if (lane == 0) mbar_arrive_expect_tx(mbar, cnt * d * 4u);
+    __syncwarp();
+    if (mine)
+      bulk_row_to_smem(rows + static_cast<size_t>(ci - c0) * d,
+                       a.base + static_cast<uint64_t>(node) * d, d * 4u, mbar);
+    ok = mbar_wait_bounded(mbar, phase);
+    phase ^= 1u;
+    if (!ok) return FLT_MAX;
+    float p[ROUNDS][4];
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++) {
+#pragma unroll
+      for (int i = 0; i < 4; i++) p[r][i] = 0.0f;
+      const uint32_t c = 4u * r + g;
+      if (c < cnt) {
+        const float* row = rows + static_cast<size_t>(c) * d;
+#pragma unroll
+        for (int k = 0; k < KSTEPS; k++) {
+          const uint32_t off = 32u * k + 4u * m;
+          if (off < d) {
+            const float4 x = *reinterpret_cast<const float4*>(row + off);
+            p[r][0] = fmaf(q.v[k].x, x.x, p[r][0]);
+            p[r][1] = fmaf(q.v[k].y, x.y, p[r][1]);
+            p[r][2] = fmaf(q.v[k].z, x.z, p[r][2]);
+            p[r][3] = fmaf(q.v[k].w, x.w, p[r][3]);
+          }
+        }
+      }
+    }
+    // level xor 4 (residues +16): transposed, keeps ROUNDS/2 rounds
+    float v4[ROUNDS / 2][4];
+#pragma unroll
+    for (int i = 0; i < ROUNDS / 2; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const float send = bA ? p[i][j] : p[i + ROUNDS / 2][j];
+        const float keep = bA ? p[i + ROUNDS / 2][j] : p[i][j];
+        v4[i][j] = keep + __shfl_xor_sync(kFull, send, 4);
+      }
+    float v[4];
+    uint32_t r_of_lane;
+    if constexpr (ROUNDS == 2) {
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        float t = v4[0][j];
+        t = t + __shfl_xor_sync(kFull, t, 2);  // residues +8
+        t = t + __shfl_xor_sync(kFull, t, 1);  // residues +4
+        v[j] = t;
+      }
+      r_of_lane = bA ? 1u : 0u;
+    } else if constexpr (ROUNDS == 4) {
+      float v2[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const float send = bB ? v4[0][j] : v4[1][j];
+        const float keep = bB ? v4[1][j] : v4[0][j];
+        v2[j] = keep + __shfl_xor_sync(kFull, send, 2);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) v[j] = v2[j] + __shfl_xor_sync(kFull, v2[j], 1);
+      r_of_lane = (bA ? 2u : 0u) + (bB ? 1u : 0u);
+    } else {
+      float v2[2][4];
+#pragma unroll
+      for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const float send = bB ? v4[i][j] : v4[i + 2][j];
+          const float keep = bB ? v4[i + 2][j] : v4[i][j];
+          v2[i][j] = keep + __shfl_xor_sync(kFull, send, 2);
+        }
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const float send = bC ? v2[0][j] : v2[1][j];
+        const float keep = bC ? v2[1][j] : v2[0][j];
+        v[j] = keep + __shfl_xor_sync(kFull, send, 1);
+      }
+      r_of_lane = m;
+    }
+    (void)r_of_lane;
+    const float total = (v[0] + v[2]) + (v[1] + v[3]);
+    // candidate lc = 4r + g sits in lane 8g + m(r): m(r) spreads r over the transposed bits
+    const uint32_t lc = mine ? ci - c0 : 0u;
+    const uint32_t r = lc >> 2;
+    uint32_t msrc;
+    if constexpr (ROUNDS == 2)
+      msrc = r << 2;
+    else if constexpr (ROUNDS == 4)
+      msrc = ((r >> 1) << 2) | ((r & 1u) << 1);
+    else
+      msrc = r;
+    const float dd = __shfl_sync(kFull, total, ((lc & 3u) << 3) | msrc);
+    if (mine) result = -dd;
+  }
+  return result;
+}
+
+}  // namespace
+
+template <int KSTEPS, int ROWS>
+__global__ void __launch_bounds__(32) k_search_m32(SearchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const uint32_t lane = lane_id();
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw);
+  uint64_t* mkey = reinterpret_cast<uint64_t*>(smem_raw + 16);   // 32 merge keys
+  uint32_t* mid = reinterpret_cast<uint32_t*>(smem_raw + 16 + 256);  // 32 merge ids
+  uint32_t* hash = reinterpret_cast<uint32_t*>(smem_raw + 16 + 256 + 128);
+  float* rows = reinterpret_cast<float*>(smem_raw + 16 + 256 + 128 + 4u * a.hash_slots);
+  const uint32_t hmask = a.hash_slots - 1u;
+  const uint32_t kp = a.kp, kd = a.kd;
+  constexpr uint32_t L = 64;
+  if (lane == 0) mbar_init(mbar, 1);
+  __syncwarp();
+  uint32_t phase = 0;
+  unsigned long long ev = 0, it_all = 0;
+  bool ok = true;
+  const uint32_t m = lane & 7u;
+  const uint32_t e_of_lane = lane / kd, nb_of_lane = lane % kd;
+
+  for (;;) {
+    uint32_t qi = 0;
+    if (lane == 0) qi = atomicAdd(a.work, 1u);
+    qi = __shfl_sync(kFull, qi, 0);
+    if (qi >= a.n) break;
+    const uint32_t qid = a.order ? a.order[qi] : qi;
+    const float* qrow = a.base + static_cast<uint64_t>(qid) * a.d;
+    Q4<KSTEPS> q;
+#pragma unroll
+    for (int k = 0; k < KSTEPS; k++) {
+      const uint32_t off = 32u * k + 4u * m;
+      q.v[k] = (off < a.d) ? __ldg(reinterpret_cast<const float4*>(qrow + off))
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    // list before the last merge (top) and the last candidates (cand): the full 64-entry list
+    // is their sorted union
+    uint64_t top_key = pack_key(FLT_MAX, lane);
+    uint32_t top_id = kTomb;
+    uint64_t cand_key;
+    uint32_t cand_id;
+    {  // seeds: every slot is scored (Gsearcher.cuh:958-976 has no visited test)
+      const uint32_t node = static_cast<uint32_t>((a.seed_base + static_cast<uint64_t>(lane)) % a.n);
+      const float dist = score_passes<KSTEPS, ROWS>(a, q, node, true, rows, mbar, phase, ok);
+      if (!ok) break;
+      cand_key = pack_key(dist, 32u + lane);
+      cand_id = node;
+      ev += (lane == 0) ? 32u : 0u;
+    }
+    // current sorted top 32 after merging the seeds
+    uint64_t cur_key;
+    uint32_t cur_id;
+    {
+      uint64_t k2[2] = {top_key, cand_key};
+      uint32_t i2[2] = {top_id, cand_id};
+      warp_sort_kv<2>(k2, i2);
+      cur_key = k2[0];
+      cur_id = i2[0];
+    }
+    hash_clear(hash, a.hash_slots);
+    __syncwarp();
+    hash_insert(hash, hmask, cur_id & kMaskedTomb);
+    __syncwarp();
+
+    uint32_t iter = 0, total = 0;
+    for (;;) {
+      // collect_top_p_normal: first kp unexplored of the top 32, marked explored
+      const bool unexp = (cur_id & kParent) == 0;
+      const unsigned umask = __ballot_sync(kFull, unexp);
+      const uint32_t found = __popc(umask);
+      if (found == 0) break;
+      const uint32_t rank = __popc(umask & ((1u << lane) - 1u));
+      uint32_t src = 0;
+      const bool want = lane < kp && lane < found;
+      if (want) {
+        unsigned mm = umask;
+        for (uint32_t i = 0; i < lane; i++) mm &= mm - 1u;
+        src = static_cast<uint32_t>(__ffs(static_cast<int>(mm)) - 1);
+      }
+      const uint32_t got = __shfl_sync(kFull, cur_id, src);
+      const uint32_t ex_lane = want ? got : kTomb;
+      if (unexp && rank < kp) cur_id |= kParent;
+      if (++total > a.max_iters) {
+        if (lane == 0) raise_error(a.status, kErrIterCap);
+        // the output is the list of the last completed merge
+        break;
+      }
+      const uint32_t ex = __shfl_sync(kFull, ex_lane, e_of_lane);
+      uint32_t node = kTomb;
+      if (ex < a.n)
+        node = a.graph[static_cast<uint64_t>(ex) * a.graph_degree + nb_of_lane];
+      else if (ex != kTomb)
+        raise_error(a.status, kErrCapacity);
+      if (node >= a.n && node != kTomb) {
+        raise_error(a.status, kErrBadId);
+        node = kTomb;
+      }
+      const bool valid = node != kTomb;
+      const unsigned same = __match_any_sync(kFull, node);
+      const bool first = lane == static_cast<uint32_t>(__ffs(static_cast<int>(same)) - 1);
+      const bool newc = valid && first && !hash_contains(hash, hmask, node);
+      __syncwarp();
+      if (newc) hash_insert(hash, hmask, node);
+      __syncwarp();
+      const float dist = score_passes<KSTEPS, ROWS>(a, q, node, newc, rows, mbar, phase, ok);
+      if (!ok) break;
+      const unsigned scored = __ballot_sync(kFull, newc);
+      ev += (lane == 0) ? __popc(scored) : 0u;
+      // the list that this merge sorts: top (positions 0..31) + candidates (32..63)
+      top_key = (cur_key & 0xFFFFFFFF00000000ull) | lane;
+      top_id = cur_id;
+      cand_key = pack_key(newc ? dist : FLT_MAX, 32u + lane);
+      cand_id = node;
+      // merge by rank: only scored candidates can enter the top (the others carry FLT_MAX and
+      // positions after every retained entry)
+      uint32_t shift = 0, cpos = 0xFFFFFFFFu;
+      unsigned rem = scored;
+      while (rem) {
+        const uint32_t c = static_cast<uint32_t>(__ffs(static_cast<int>(rem)) - 1);
+        rem &= rem - 1u;
+        const uint64_t kc = __shfl_sync(kFull, cand_key, c);
+        const uint32_t below_top = __popc(__ballot_sync(kFull, top_key < kc));
+        const uint32_t below_cand = __popc(__ballot_sync(kFull, newc && cand_key < kc));
+        if (lane == c) cpos = below_top + below_cand;
+        shift += (top_key > kc) ? 1u : 0u;
+      }
+      const uint32_t tpos = lane + shift;
+      if (tpos < 32) {
+        mkey[tpos] = top_key;
+        mid[tpos] = top_id;
+      }
+      if (cpos < 32) {
+        mkey[cpos] = cand_key;
+        mid[cpos] = cand_id;
+      }
+      __syncwarp();
+      cur_key = mkey[lane];
+      cur_id = mid[lane];
+      __syncwarp();
+      if (++iter == a.reset_iter) {
+        hash_clear(hash, a.hash_slots);
+        __syncwarp();
+        hash_insert(hash, hmask, cur_id & kMaskedTomb);
+        __syncwarp();
+        iter = 0;
+      }
+    }
+    if (!ok) break;
+    it_all += (lane == 0) ? total : 0u;
+    uint64_t k2[2] = {top_key, cand_key};
+    uint32_t i2[2] = {top_id, cand_id};
+    warp_sort_kv<2>(k2, i2);
+    uint32_t* orow = a.out + static_cast<uint64_t>(qid) * L;
+    orow[lane] = i2[0] & kMaskedTomb;
+    orow[32 + lane] = i2[1] & kMaskedTomb;
+  }
+  if (!ok) {
+    if (lane == 0) raise_error(a.status, kErrWait);
+    mbar_wait_bounded(mbar, phase ^ 1u);
+  }
+  if (lane == 0) {
+    if (ev) atomicAdd(a.evals, ev);
+    if (it_all) atomicAdd(a.iters, it_all);
+  }
+}
+
+constexpr int kM32Rows = 8;
+
+size_t search_m32_smem(uint32_t d, uint32_t hash_slots) {
+  return 16 + 256 + 128 + 4 * static_cast<size_t>(hash_slots) +
+         static_cast<size_t>(kM32Rows) * 4 * d;
+}
+
+template <int KS>
+static cudaError_t launch_search_m32(const SearchArgs& a, int num_sms, size_t smem_optin,
+                                     cudaStream_t st) {
+  const size_t smem = search_m32_smem(a.d, a.hash_slots);
+  if (smem > smem_optin) return cudaErrorInvalidValue;
+  auto kern = k_search_m32<KS, kM32Rows>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  uint64_t blocks = static_cast<uint64_t>(num_sms) * per_sm;
+  if (blocks > a.n) blocks = a.n;
+  kern<<<static_cast<unsigned>(blocks), 32, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 bool search_supported(uint32_t d, uint32_t km, uint32_t kp, uint32_t kd) {
   return d > 0 && d <= 512 && (d % 4) == 0 && kp * kd == 32 && kp >= 1 && km >= 32 &&
          km <= 96 && (km % 32) == 0;
@@ -386,8 +708,8 @@ cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, c
   const bool small = a.d <= 256;
   switch (km_s) {
     case 1:
-      return small ? launch_search_t<1, 8>(a, num_sms, smem_optin, st)
-                   : launch_search_t<1, 16>(a, num_sms, smem_optin, st);
+      return small ? launch_search_m32<8>(a, num_sms, smem_optin, st)
+                   : launch_search_m32<16>(a, num_sms, smem_optin, st);
     case 2:
       return small ? launch_search_t<2, 8>(a, num_sms, smem_optin, st)
                    : launch_search_t<2, 16>(a, num_sms, smem_optin, st);
