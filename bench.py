@@ -31,7 +31,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "distance_evals_per_s (build, 1Mx200 IP, M=32, L=64)"
+METRIC = "distance_evals_per_s (build, 1Mx200 IP, M=32, L=64, screened vs FP32, identical edges)"
 UNIT = "evals/s"
 
 
@@ -50,6 +50,9 @@ def parse():
                     help="target length of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--screen", default="bf16", choices=["bf16", "none"],
+                    help="path timed for `value`; the other one is timed beside it")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the other path")
     return ap.parse_args()
 
 
@@ -261,7 +264,10 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     base, gt = gpu_workload(args, dev)
     torch.cuda.synchronize()
-    params = pg.default_params(args.degree, args.beam)
+    screen = pg.SCREEN_BF16 if args.screen == "bf16" else pg.SCREEN_NONE
+    params = pg.default_params(args.degree, args.beam, screen=screen)
+    other = pg.default_params(args.degree, args.beam,
+                              screen=pg.SCREEN_NONE if screen else pg.SCREEN_BF16)
     n, d = base.shape
     graph = torch.empty((n, args.degree), dtype=torch.int32, device=dev)
     proj = torch.empty((n, 16), dtype=torch.int32, device=dev)
@@ -287,6 +293,28 @@ def run_ours(args):
         barrier(world)
     ms_total = start.elapsed_time(stop)
     ms_total = allmax(ms_total, world)
+    # the other path (plain FP32 when the screened path is timed), same inputs, and the check
+    # that both give identical edges
+    other_line = None
+    if not args.no_plain:
+        graph2 = torch.empty_like(graph)
+        proj2 = torch.empty_like(proj)
+        h.build_device(base, gt, graph2, proj2, other)
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        k2 = max(1, min(args.steps, 3))
+        t0.record(stream)
+        for _ in range(k2):
+            ost = h.build_device(base, gt, graph2, proj2, other)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        oms = t0.elapsed_time(t1) / k2
+        other_line = {"screen": "none" if screen else "bf16", "ms_per_step": round(oms, 3),
+                      "value": ost.evals_total / (oms / 1e3),
+                      "identical_edges": bool(torch.equal(graph, graph2) and torch.equal(proj, proj2)),
+                      "speedup_of_timed_path": round(oms / (ms_total / args.steps), 3)}
+        del graph2, proj2
     evals = stats[-1].evals_total
     assert all(s.evals_total == evals for s in stats), "evaluation count changed between builds"
     value = evals * args.steps * world / (ms_total / 1e3)
@@ -332,7 +360,7 @@ def run_ours(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32",
+                "dtype": "f32" if args.screen == "none" else "f32+bf16",
                 "data": "synthetic (seeded mixture-of-Gaussians stand-in for T2I-style data)",
                 "config": {"workload": f"ParaGraph build {args.n}x{args.d} IP, gt top-128, "
                                        f"M={args.degree}, L={args.beam}",
@@ -346,6 +374,9 @@ def run_ours(args):
                              "search": [round(x, 2) for x in list(s.ms_search)[:params.link_rounds]],
                              "prune": [round(x, 2) for x in list(s.ms_prune)[:params.link_rounds]],
                              "merge": [round(x, 2) for x in list(s.ms_merge)[:params.link_rounds]]},
+                "screen": args.screen,
+                "rescored": list(s.rescored)[:params.link_rounds],
+                "other_path": other_line,
                 "gpu_launches": launches_per_build * args.steps,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary()}

@@ -45,7 +45,8 @@ enum Counter {
   C_PRUNE = 6,    // + round
   C_MERGE = 10,   // + round
   C_ITERS = 14,   // + round
-  C_COUNT = 18
+  C_RESCORED = 18,  // + round
+  C_COUNT = 22
 };
 
 struct Workspace {
@@ -188,8 +189,9 @@ int check_params(const pg_params* p, uint64_t n, uint32_t d, uint64_t q) {
     if (p->kd > p->proj_degree || p->kd > p->degree)
       return fail(PG_EINVAL, "kd=%u exceeds a graph degree", p->kd);
   }
-  if (p->screen != PG_SCREEN_NONE)
-    return fail(PG_EUNSUPPORTED, "screened builds are not available in this build");
+  if (p->screen != PG_SCREEN_NONE && p->screen != PG_SCREEN_BF16)
+    return fail(PG_EUNSUPPORTED, "screen=%u: only PG_SCREEN_NONE and PG_SCREEN_BF16 are built",
+                p->screen);
   return PG_OK;
 }
 
@@ -317,7 +319,11 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
     pr.sorted = nullptr;
     pr.evals = cnt + C_PRUNE + r;
     pr.status = h->d_status;
-    PG_CUDA(pg::launch_prune_reverse(pr, false, sms, s));
+    pr.rescored = cnt + C_RESCORED + r;
+    if (p->screen == PG_SCREEN_BF16 && pg::screen_supported(pr.c, d, pr.strict))
+      PG_CUDA(pg::launch_prune_screen(pr, sms, h->smem_optin, s));
+    else
+      PG_CUDA(pg::launch_prune_reverse(pr, false, sms, s));
     PG_CUDA(pg::launch_reverse_csr(pruned, pnum, p->degree, n, indeg, offs, tsum, cursor, edges,
                                    sms, s));
     PG_CUDA(pg::launch_reverse_lists(offs, edges, n, p->link_reverse, rev, rnum, sms, s));
@@ -364,6 +370,7 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
       st->evals_prune[r] = c[C_PRUNE + r];
       st->evals_merge[r] = c[C_MERGE + r];
       st->search_iters[r] = c[C_ITERS + r];
+      st->rescored[r] = c[C_RESCORED + r];
       st->evals_total += c[C_SEARCH + r] + c[C_PRUNE + r] + c[C_MERGE + r];
     }
     float ms = 0;

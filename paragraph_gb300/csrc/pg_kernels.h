@@ -22,6 +22,7 @@ struct PruneArgs {
   uint32_t* sorted;        // optional n x c: candidate rows after the sort
   unsigned long long* evals;
   uint32_t* status;        // error flags (kErr*)
+  unsigned long long* rescored;  // screened kernel: occlusion tests re-scored exactly (nullable)
 };
 
 struct MergeArgs {
@@ -78,6 +79,11 @@ cudaError_t launch_merge_prune(const MergeArgs& a, int num_sms, cudaStream_t st)
 // (see search_supported).
 cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, cudaStream_t st);
 bool search_supported(uint32_t d, uint32_t km, uint32_t kp, uint32_t kd);
+// Screened (BF16 tensor-core Gram + exact re-scoring) prune for strict rounds, c <= 64, d <= 256.
+bool screen_supported(uint32_t c, uint32_t d, int strict);
+size_t screen_smem_per_warp(uint32_t d);
+cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_optin,
+                                cudaStream_t st);
 size_t search_smem_per_warp(uint32_t d, uint32_t hash_slots);
 
 constexpr uint32_t kScanTileElems = 4096;

@@ -1,0 +1,318 @@
+// pg_screen.cu -- screened prune + reverse (K6/K10) with a BF16 tensor-core Gram.
+//
+// Same result as k_prune_reverse (strict rounds), bit for bit.  Per node (one warp):
+//   1. one pass over the candidate rows: each lane runs the exact FP32 chain dist(b, c) for its
+//      candidates (distance_between's order, Gbuilder.cuh:785-797) and, from the same loads,
+//      rounds the row to BF16 and accumulates two norms per row, |x| and |x - bf16(x)|;
+//   2. the candidate Gram G = A A^T (A = the BF16 rows, C x Dp, Dp = D rounded up to 16) on the
+//      tensor cores (m16n8k16 BF16 MMA, FP32 accumulation), streamed: each 16-wide K chunk of the
+//      BF16 rows goes through a 3 KB shared buffer straight into the MMAs, and the 20 m16n8
+//      tiles of the lower triangle accumulate in registers; G is kept packed (strictly lower);
+//   3. the RNG scan of the plain kernel, where each occlusion test dist(p, r) < d_p is decided
+//      from -G[p][r] when it lies farther than the error bound E(p, r) from d_p, and re-scored
+//      with the exact FP32 chain otherwise.
+// Error bound (x, y = FP32 rows, x^ = bf16(x), e_x = x - x^; Cauchy-Schwarz throughout):
+//   |sum x^y^ - sum xy| <= |e_x|(|y| + |e_y|) + |x||e_y|
+//   |MMA(x^, y^) - sum x^y^| <= c_acc (|x| + |e_x|)(|y| + |e_y|)   (FP32 accumulation of Dp terms)
+//   |chain(x, y) - sum xy| <= c_seq |x||y|                          (the reference's FP32 chain)
+// with c_acc = (Dp + 32) * 2^-21 and c_seq = (D + 2) * 2^-23 (both several times the textbook
+// gamma_n), plus a 2^-20 relative guard on the comparison itself.
+#include <cuda_bf16.h>
+
+#include "pg_device.cuh"
+#include "pg_kernels.h"
+
+namespace pg {
+
+namespace {
+
+constexpr int kScrC = 64;  // candidates per node handled by the screened kernel
+
+__device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi, float& elo, float& ehi) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+  elo = lo - __low2float(h);
+  ehi = hi - __high2float(h);
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
+  const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+
+__device__ __forceinline__ void ldsm_x2(uint32_t (&r)[2], const void* p) {
+  const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];"
+               : "=r"(r[0]), "=r"(r[1])
+               : "r"(a));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4],
+                                         const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ float key_to_dist(uint64_t key) {
+  const uint32_t o = static_cast<uint32_t>(key >> 32);
+  const uint32_t u = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
+  return __uint_as_float(u);
+}
+
+__host__ __device__ inline uint32_t screen_dp(uint32_t d) { return (d + 15u) / 16u * 16u; }
+
+}  // namespace
+
+constexpr uint32_t kChunkStride = 24;  // BF16 per chunk row: 48 B keeps ldmatrix rows conflict-free
+constexpr uint32_t kTri = kScrC * (kScrC - 1) / 2;  // packed strictly-lower Gram entries
+
+// bytes of shared memory per warp
+size_t screen_smem_per_warp(uint32_t /*d*/) {
+  return static_cast<size_t>(kScrC) * kChunkStride * 2  // one K chunk of the BF16 rows
+         + static_cast<size_t>(kTri) * 4                 // G, strictly lower triangle
+         + static_cast<size_t>(kScrC) * 4 * 7;           // ids, dist, |x|, |e|, slot, kept x2
+}
+
+bool screen_supported(uint32_t c, uint32_t d, int strict) {
+  return strict && c <= static_cast<uint32_t>(kScrC) && d >= 4 && d <= 1024 && (d % 4) == 0;
+}
+
+__device__ __forceinline__ uint32_t tri_index(uint32_t r, uint32_t c) {  // r > c
+  return r * (r - 1) / 2 + c;
+}
+
+__global__ void __launch_bounds__(32, 16) k_prune_screen(PruneArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const uint32_t lane = lane_id();
+  const uint32_t d = a.d;
+  const uint32_t dp = screen_dp(d);
+  __nv_bfloat16* Ck = reinterpret_cast<__nv_bfloat16*>(smem_raw);
+  float* G = reinterpret_cast<float*>(smem_raw + static_cast<size_t>(kScrC) * kChunkStride * 2);
+  uint32_t* ids_s = reinterpret_cast<uint32_t*>(G + kTri);
+  float* dist_s = reinterpret_cast<float*>(ids_s + kScrC);
+  float* nrm_s = dist_s + kScrC;   // |x| per original candidate slot
+  float* err_s = nrm_s + kScrC;    // |x - bf16(x)|
+  uint32_t* orig_s = reinterpret_cast<uint32_t*>(err_s + kScrC);  // sorted -> original slot
+  uint32_t* kept_o = orig_s + kScrC;  // kept: original slot
+  uint32_t* kept_i = kept_o + kScrC;  // kept: id
+  const float c_acc = static_cast<float>(dp + 32) * 4.76837158e-07f;  // 2^-21
+  const float c_seq = static_cast<float>(d + 2) * 1.19209290e-07f;    // 2^-23
+  const uint32_t g = lane >> 2, t4 = lane & 3u;
+  uint64_t ev = 0, resc = 0;
+
+  for (uint64_t b = blockIdx.x; b < a.n; b += gridDim.x) {
+    const float* brow = a.base + b * d;
+    uint32_t id[2];
+    bool valid[2];
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+      uint32_t x = (j < a.c) ? a.graph[b * a.c + j] : kTomb;
+      if (x >= a.n && x != kTomb && x != kMaskedTomb) {
+        raise_error(a.status, kErrBadId);
+        x = kTomb;
+      }
+      id[s] = x;
+      valid[s] = (x != kTomb && x != static_cast<uint32_t>(b) && x != kMaskedTomb);
+    }
+    const float4* b4 = reinterpret_cast<const float4*>(brow);
+    const float4* r4[2];
+#pragma unroll
+    for (int s = 0; s < 2; s++)
+      r4[s] = reinterpret_cast<const float4*>(valid[s] ? a.base + static_cast<uint64_t>(id[s]) * d
+                                                       : brow);
+    float acc[2] = {0.f, 0.f}, nn[2] = {0.f, 0.f}, ee[2] = {0.f, 0.f};
+    float gm[20][4];  // lower-triangle m16n8 tiles: tile (mt, nt) at mt*(mt+1) + nt, nt <= 2mt+1
+#pragma unroll
+    for (int i = 0; i < 20; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) gm[i][j] = 0.f;
+    const uint32_t n4 = d >> 2;
+    // ---- 1+2. stream K in chunks of 16: exact chains, BF16 chunk, MMA on the chunk
+    for (uint32_t k0 = 0; k0 < dp; k0 += 16) {
+#pragma unroll
+      for (uint32_t q = 0; q < 4; q++) {
+        const uint32_t i = (k0 >> 2) + q;  // float4 index
+        const bool in = i < n4;
+        const float4 u = in ? __ldg(b4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+          const float4 v = in ? __ldg(r4[s] + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+          uint2 packed = make_uint2(0u, 0u);
+          if (in) {
+            acc[s] = fmaf(u.x, v.x, acc[s]);
+            acc[s] = fmaf(u.y, v.y, acc[s]);
+            acc[s] = fmaf(u.z, v.z, acc[s]);
+            acc[s] = fmaf(u.w, v.w, acc[s]);
+            float e0, e1, e2, e3;
+            packed.x = bf16x2_bits(v.x, v.y, e0, e1);
+            packed.y = bf16x2_bits(v.z, v.w, e2, e3);
+            nn[s] = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, nn[s]))));
+            ee[s] = fmaf(e0, e0, fmaf(e1, e1, fmaf(e2, e2, fmaf(e3, e3, ee[s]))));
+          }
+          const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+          *reinterpret_cast<uint2*>(Ck + j * kChunkStride + 4 * q) =
+              valid[s] ? packed : make_uint2(0u, 0u);
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int mt = 0; mt < 4; mt++) {
+        uint32_t af[4];
+        ldsm_x4(af, Ck + (16 * mt + (lane & 15u)) * kChunkStride + (lane >> 4) * 8);
+#pragma unroll
+        for (int nt = 0; nt <= 2 * mt + 1; nt++) {
+          uint32_t bf[2];
+          ldsm_x2(bf, Ck + (8 * nt + (lane & 7u)) * kChunkStride + ((lane >> 3) & 1u) * 8);
+          mma_bf16(gm[mt * (mt + 1) + nt], af, bf);
+        }
+      }
+      __syncwarp();
+    }
+#pragma unroll
+    for (int mt = 0; mt < 4; mt++)
+#pragma unroll
+      for (int nt = 0; nt <= 2 * mt + 1; nt++) {
+        const float* c = gm[mt * (mt + 1) + nt];
+        const uint32_t r0 = 16 * mt + g, c0 = 8 * nt + 2 * t4;
+        if (r0 > c0) G[tri_index(r0, c0)] = c[0];
+        if (r0 > c0 + 1) G[tri_index(r0, c0 + 1)] = c[1];
+        if (r0 + 8 > c0) G[tri_index(r0 + 8, c0)] = c[2];
+        if (r0 + 8 > c0 + 1) G[tri_index(r0 + 8, c0 + 1)] = c[3];
+      }
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+      nrm_s[j] = valid[s] ? sqrtf(nn[s]) * 1.0001f : 0.f;
+      err_s[j] = valid[s] ? sqrtf(ee[s]) * 1.0001f : 0.f;
+    }
+    float dist[2];
+#pragma unroll
+    for (int s = 0; s < 2; s++) dist[s] = valid[s] ? -acc[s] : FLT_MAX;
+    const unsigned v0 = __ballot_sync(kFull, valid[0]);  // every lane takes part
+    const unsigned v1 = __ballot_sync(kFull, valid[1]);
+    ev += (lane == 0) ? (__popc(v0) + __popc(v1)) : 0u;
+
+    // ---- sort by (exact distance, slot): the stable order of bubble_sort
+    uint64_t key[2];
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+      key[s] = (j < a.c) ? pack_key(dist[s], j) : ~0ull;
+    }
+    warp_sort_kv<2>(key, id);
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+      const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
+      if (i < a.c) {
+        ids_s[i] = id[s];
+        dist_s[i] = key_to_dist(key[s]);
+        orig_s[i] = key_pos(key[s]);
+      }
+    }
+    __syncwarp();
+
+    // ---- 3. screened RNG scan
+    const uint32_t first = ids_s[0];
+    if (first == kTomb || first == kMaskedTomb) {
+      if (lane == 0) a.pruned_num[b] = 0;
+      __syncwarp();
+      continue;
+    }
+    if (lane == 0) {
+      kept_o[0] = orig_s[0];
+      kept_i[0] = first;
+    }
+    __syncwarp();
+    uint32_t k = 0;
+    uint64_t checks = 0;
+    for (uint32_t j = 1; j < a.c; j++) {
+      const uint32_t p = ids_s[j];
+      if (p == kTomb || p == kMaskedTomb) break;
+      const float dpj = dist_s[j];
+      const uint32_t po = orig_s[j];
+      const float np = nrm_s[po], ep = err_s[po];
+      bool occ = false;
+      for (uint32_t t0 = 0; t0 <= k; t0 += 32) {
+        const uint32_t t = t0 + lane;
+        bool yes = false, amb = false;
+        if (t <= k) {
+          const uint32_t ro = kept_o[t];
+          const float nr = nrm_s[ro], er = err_s[ro];
+          const float dhat = -G[po > ro ? tri_index(po, ro) : tri_index(ro, po)];
+          const float bound = ep * (nr + er) + np * er + c_acc * (np + ep) * (nr + er) +
+                              c_seq * np * nr + fabsf(dhat) * 9.5367431640625e-07f + 1e-30f;
+          if (dhat + bound < dpj)
+            yes = true;
+          else if (!(dhat - bound >= dpj))
+            amb = true;
+        }
+        unsigned m_yes = __ballot_sync(kFull, yes);
+        const unsigned m_amb = __ballot_sync(kFull, amb);
+        const unsigned before = m_yes ? ((m_yes & (0u - m_yes)) - 1u) : 0xFFFFFFFFu;
+        const unsigned need = m_amb & before;
+        if (need) {
+          bool ex = false;
+          if ((need >> lane) & 1u)
+            ex = dist_seq(a.base + static_cast<uint64_t>(p) * d,
+                          a.base + static_cast<uint64_t>(kept_i[t]) * d, d) < dpj;
+          m_yes |= __ballot_sync(kFull, ex);
+          resc += (lane == 0) ? __popc(need) : 0u;
+        }
+        if (m_yes) {
+          checks += static_cast<uint32_t>(__ffs(static_cast<int>(m_yes)));
+          occ = true;
+          break;
+        }
+        checks += min(32u, k + 1 - t0);
+      }
+      if (!occ) {
+        k++;
+        if (lane == 0) {
+          kept_o[k] = po;
+          kept_i[k] = p;
+        }
+        __syncwarp();
+        if (k == a.p - 1) break;
+      }
+    }
+    ev += (lane == 0) ? checks : 0;
+    const uint32_t cnt = k + 1;
+    if (lane == 0) a.pruned_num[b] = cnt;
+    for (uint32_t t = lane; t < cnt; t += 32) {
+      const uint32_t dst = kept_i[t];
+      a.pruned[b * a.p + t] = dst;
+      atomicAdd(a.indeg + dst, 1u);
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    if (ev) atomicAdd(a.evals, static_cast<unsigned long long>(ev));
+    if (resc && a.rescored) atomicAdd(a.rescored, static_cast<unsigned long long>(resc));
+  }
+}
+
+cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_optin,
+                                cudaStream_t st) {
+  if (!screen_supported(a.c, a.d, a.strict)) return cudaErrorInvalidValue;
+  const size_t smem = screen_smem_per_warp(a.d);
+  if (smem > smem_optin) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_prune_screen, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_prune_screen, 32, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  uint64_t blocks = static_cast<uint64_t>(num_sms) * per_sm;
+  if (blocks > a.n) blocks = a.n;
+  k_prune_screen<<<static_cast<unsigned>(blocks), 32, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace pg

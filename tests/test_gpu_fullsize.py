@@ -53,3 +53,21 @@ def test_full_size_build_matches_oracle(workload):
     assert (g1[valid] < N).all()
     assert not (g1 == np.arange(N, dtype=np.uint32)[:, None]).any()
     assert valid.sum(axis=1).max() <= 32
+
+
+def test_full_size_screened_build_is_identical(workload):
+    import paragraph_gb300 as pg
+    base, gt = workload
+    outs = []
+    stats = []
+    with pg.Handle(0) as h:
+        for screen in (pg.SCREEN_NONE, pg.SCREEN_BF16):
+            graph = torch.empty((N, 32), dtype=torch.int32, device="cuda")
+            proj = torch.empty((N, 16), dtype=torch.int32, device="cuda")
+            stats.append(h.build_device(base, gt, graph, proj, pg.default_params(32, 64, screen=screen)))
+            outs.append((graph.cpu().numpy(), proj.cpu().numpy()))
+    assert np.array_equal(outs[0][1], outs[1][1])
+    bad = (outs[0][0] != outs[1][0]).any(axis=1)
+    assert not bad.any(), f"{bad.sum()} rows differ between the plain and the screened build"
+    assert stats[0].evals_total == stats[1].evals_total
+    print("rescored", list(stats[1].rescored)[:2], "of", list(stats[1].evals_prune)[:2])

@@ -136,11 +136,12 @@ def test_search_beam_widths_match_oracle(handle, km):
     assert (ev, it) == (rev, rit)
 
 
-def _build_both(pg, handle, base, gt, degree=32, beam=64):
+def _build_both(pg, handle, base, gt, degree=32, beam=64, screen=0):
     n, d = base.shape
     graph = empty_u32(n, degree)
     proj = empty_u32(n, 16)
-    st = handle.build_device(dev_f32(base), dev_u32(gt), graph, proj, pg.default_params(degree, beam))
+    st = handle.build_device(dev_f32(base), dev_u32(gt), graph, proj,
+                             pg.default_params(degree, beam, screen=screen))
     ref = oracle.build_graph(base, gt, degree=degree, beam=beam)
     return host_u32(graph), host_u32(proj), st, ref
 
@@ -224,3 +225,33 @@ def test_unsupported_shapes_are_rejected(pg, handle):
     with pytest.raises(pg.PGError) as e:
         handle.build_device(dev_f32(base), dev_u32(gt), empty_u32(100, 32), None)
     assert e.value.code == pg.PG_EUNSUPPORTED
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_screened_build_matches_plain_and_oracle_fixture(pg, handle, golden_dir, case):
+    f = load(golden_dir, case)
+    g, p, st, ref = _build_both(pg, handle, f["base"], f["gt"], screen=pg.SCREEN_BF16)
+    assert np.array_equal(p, ref["proj"])
+    assert np.array_equal(g, ref["graph"])
+    assert st.evals_total == ref["stats"]["evals_total"]
+
+
+@pytest.mark.parametrize("n,d,seed", [(20000, 200, 1), (6000, 64, 7), (3000, 8, 8)])
+def test_screened_build_matches_oracle(pg, handle, n, d, seed):
+    from paragraph_gb300 import datagen
+    base, gt = datagen.make_dataset(n, d, seed=seed)
+    g, p, st, ref = _build_both(pg, handle, base, gt, screen=pg.SCREEN_BF16)
+    assert np.array_equal(p, ref["proj"])
+    bad = (g != ref["graph"]).any(axis=1)
+    assert not bad.any(), f"{bad.sum()} rows differ"
+    assert st.evals_total == ref["stats"]["evals_total"]
+    # the screen decides most occlusion tests without the exact chain
+    assert sum(st.rescored) < 0.5 * sum(st.evals_prune)
+
+
+def test_screened_build_with_hubs_and_duplicates(pg, handle, golden_dir):
+    """Exact duplicate vectors give exact ties and zero-width gaps: the screen must defer every
+    such decision to the exact chain."""
+    f = load(golden_dir, "edge")
+    g, p, st, ref = _build_both(pg, handle, f["base"], f["gt"], screen=pg.SCREEN_BF16)
+    assert np.array_equal(g, ref["graph"])
