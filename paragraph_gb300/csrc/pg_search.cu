@@ -484,7 +484,7 @@ __device__ __forceinline__ float score_passes(const SearchArgs& a, const Q4<KSTE
 }  // namespace
 
 template <int KSTEPS, int ROWS>
-__global__ void __launch_bounds__(32) k_search_m32(SearchArgs a) {
+__global__ void __launch_bounds__(32, 20) k_search_m32(SearchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const uint32_t lane = lane_id();
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw);
