@@ -71,6 +71,10 @@ typedef struct pg_params {
 /* Ids are always range-checked on the device: an id >= n that is not tomb is replaced by tomb,
  * never read, and the call returns PG_EINVAL.  The flag is accepted for compatibility. */
 #define PG_FLAG_VALIDATE_INPUT 1u
+/* Capture the whole build (every launch, memset and copy) in a CUDA graph on the handle's stream
+ * the first time, and replay that graph on later builds with identical parameters, buffers and
+ * sub-index table.  Needs a handle created with a non-default stream; ignored otherwise. */
+#define PG_FLAG_CUDA_GRAPH 2u
 
 /* Per-build statistics.  A distance evaluation is one call of the reference's
  * distance_between (Gbuilder.cuh:785-797) or one search distance (Gsearcher.cuh:1016-1036),
@@ -113,6 +117,19 @@ int pg_build_host(pg_handle h, const pg_params* p, const float* base, uint64_t n
 int pg_build_device(pg_handle h, const pg_params* p, const float* d_base, uint64_t n,
                     uint32_t d, const uint32_t* d_gt, uint64_t q, uint32_t* d_graph,
                     uint32_t* d_proj, pg_stats* st);
+
+/* Batched build of `count` independent sub-indexes (uneven sizes) in one pass of the pipeline:
+ * every stage is one launch over all sub-indexes' points, and the beam search's work queue spans
+ * them all.  Sub-index i owns points [node_off[i], node_off[i+1]) of d_base (all vectors
+ * concatenated) and ground-truth rows [query_off[i], query_off[i+1]) of d_gt, whose ids are local
+ * to it (0 .. n_i - 1); entry points are drawn inside each sub-index.  Outputs (concatenated like
+ * the inputs, ids local to their sub-index) equal building each sub-index alone.  node_off and
+ * query_off are host arrays of count + 1 ascending offsets starting at 0.  This is the batched
+ * form of pg_build_device; the reference builds one index per driver run. */
+int pg_build_batched_device(pg_handle h, const pg_params* p, const float* d_base, uint32_t d,
+                            const uint32_t* d_gt, const uint64_t* node_off,
+                            const uint64_t* query_off, uint32_t count, uint32_t* d_graph,
+                            uint32_t* d_proj, pg_stats* st);
 
 /* ---- stages: one entry point per reference kernel, device pointers, handle's stream ------ */
 /* K0 match_top1_kernel_v0 (Gbuilder.cuh:104-135, launched tests/test_t2iend.cu:976): for each

@@ -26,6 +26,7 @@ TOMB = 0xFFFFFFFF
 PG_OK, PG_EINVAL, PG_ECUDA, PG_ENOMEM, PG_ETIMEOUT, PG_EUNSUPPORTED, PG_EIO = range(7)
 SCREEN_NONE, SCREEN_BF16, SCREEN_FP8 = 0, 1, 2
 FLAG_VALIDATE_INPUT = 1
+FLAG_CUDA_GRAPH = 2
 
 _ERRNAMES = {1: "PG_EINVAL", 2: "PG_ECUDA", 3: "PG_ENOMEM", 4: "PG_ETIMEOUT",
              5: "PG_EUNSUPPORTED", 6: "PG_EIO"}
@@ -88,6 +89,8 @@ SIGNATURES = {
                                      _VP, _VP, ctypes.POINTER(Stats)]),
     "pg_build_device": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _U64, _U32, _VP, _U64,
                                        _VP, _VP, ctypes.POINTER(Stats)]),
+    "pg_build_batched_device": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _U32, _VP, _VP,
+                                               _VP, _U32, _VP, _VP, ctypes.POINTER(Stats)]),
     "pg_match_top1": (ctypes.c_int, [_VP, _VP, _U64, _U32, _U64, _VP]),
     "pg_prune_reverse": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _U32, _U32, _U32, ctypes.c_int,
                                         _VP, _VP, _VP, _VP, _VP, _U64P]),
@@ -216,6 +219,20 @@ class Handle:
         st = Stats()
         _check(lib().pg_build_device(self._h, ctypes.byref(params), _ptr(base), n, d, _ptr(gt),
                                      gt.shape[0], _ptr(graph), _ptr(proj), ctypes.byref(st)))
+        return st
+
+    def build_batched(self, base, gt, node_off, query_off, graph, proj=None,
+                      params: Params | None = None) -> Stats:
+        """pg_build_batched_device: base/gt/graph/proj are concatenated device tensors, the
+        offsets host sequences (count + 1 entries)."""
+        params = params or default_params()
+        no = np.ascontiguousarray(node_off, dtype=np.uint64)
+        qo = np.ascontiguousarray(query_off, dtype=np.uint64)
+        st = Stats()
+        _check(lib().pg_build_batched_device(self._h, ctypes.byref(params), _ptr(base),
+                                             base.shape[1], _ptr(gt), no.ctypes.data,
+                                             qo.ctypes.data, len(no) - 1, _ptr(graph), _ptr(proj),
+                                             ctypes.byref(st)))
         return st
 
     # ---- stages (reference kernels)

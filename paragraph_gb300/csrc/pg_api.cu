@@ -69,11 +69,11 @@ size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
 struct Layout {
   size_t winner, pruned, pruned_num, indeg, offs, tile_sums, cursor, edges, rev, rev_num, sres,
-      proj, graph, total;
+      proj, graph, segs, total;
 };
 
 Layout make_layout(uint64_t n, uint32_t pmax, uint32_t rmax, uint32_t L, uint32_t proj_deg,
-                   uint32_t degree) {
+                   uint32_t degree, uint32_t seg_count = 0) {
   Layout l{};
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -94,9 +94,24 @@ Layout make_layout(uint64_t n, uint32_t pmax, uint32_t rmax, uint32_t L, uint32_
   l.sres = take(n * L * 4);
   l.proj = take(n * proj_deg * 4);
   l.graph = take(n * degree * 4);
+  l.segs = take(2 * (static_cast<size_t>(seg_count) + 1) * 8);
   l.total = o;
   return l;
 }
+
+// What a captured build depends on: replaying it is valid only for the same parameters, buffers
+// and sub-index table.
+struct GraphKey {
+  pg_params p{};
+  const void* ptrs[5] = {};
+  uint64_t n = 0, q = 0;
+  uint32_t d = 0;
+  std::vector<uint64_t> segs;
+  bool operator==(const GraphKey& o) const {
+    return std::memcmp(&p, &o.p, sizeof(p)) == 0 && std::memcmp(ptrs, o.ptrs, sizeof(ptrs)) == 0 &&
+           n == o.n && q == o.q && d == o.d && segs == o.segs;
+  }
+};
 
 }  // namespace
 
@@ -117,6 +132,10 @@ struct pg_handle_s {
   uint32_t* h_status = nullptr;  // pinned
   unsigned long long* h_counters = nullptr;
   cudaEvent_t ev[16] = {};
+  uint64_t* h_segs = nullptr;  // pinned copy of a batched build's sub-index table
+  size_t segs_cap = 0;
+  cudaGraphExec_t gexec = nullptr;  // captured build (PG_FLAG_CUDA_GRAPH) and what it was built for
+  GraphKey gkey;
   std::mutex mu;
 };
 
@@ -124,6 +143,10 @@ namespace {
 
 int ensure_ws(pg_handle h, size_t bytes) {
   if (bytes <= h->ws_bytes) return PG_OK;
+  if (h->gexec) {  // a captured build refers to the old workspace
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
   if (h->ws) cudaFree(h->ws);
   h->ws = nullptr;
   h->ws_bytes = 0;
@@ -134,6 +157,20 @@ int ensure_ws(pg_handle h, size_t bytes) {
                 cudaGetErrorString(e));
   }
   h->ws_bytes = bytes;
+  return PG_OK;
+}
+
+int ensure_segs(pg_handle h, size_t words) {
+  if (words <= h->segs_cap) return PG_OK;
+  if (h->h_segs) cudaFreeHost(h->h_segs);
+  h->h_segs = nullptr;
+  h->segs_cap = 0;
+  cudaError_t e = cudaMallocHost(&h->h_segs, words * 8);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(PG_ENOMEM, "pinned allocation of the sub-index table failed");
+  }
+  h->segs_cap = words;
   return PG_OK;
 }
 
@@ -205,14 +242,16 @@ int status_to_error(uint32_t s) {
   return PG_OK;
 }
 
+// seg_off / qseg_off (host arrays, seg_count + 1 entries each): batched builds only.
 int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, uint32_t d,
               const uint32_t* gt, uint64_t q, uint32_t* graph_out, uint32_t* proj_out,
-              pg_stats* st) {
+              pg_stats* st, const uint64_t* seg_off = nullptr, const uint64_t* qseg_off = nullptr,
+              uint32_t seg_count = 0) {
   cudaStream_t s = h->stream;
   const uint32_t L = p->km + p->kp * p->kd;
   const uint32_t pmax = std::max(p->proj_pruned, p->degree);
   const uint32_t rmax = std::max(p->proj_reverse, p->link_reverse);
-  Layout lay = make_layout(n, pmax, rmax, L, p->proj_degree, p->degree);
+  Layout lay = make_layout(n, pmax, rmax, L, p->proj_degree, p->degree, seg_count);
   int rc = ensure_ws(h, lay.total);
   if (rc) return rc;
   char* w = h->ws;
@@ -230,133 +269,207 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
   uint32_t* proj = proj_out ? proj_out : reinterpret_cast<uint32_t*>(w + lay.proj);
   unsigned long long* cnt = h->d_counters;
   const int sms = h->num_sms;
+  uint64_t* d_seg = nullptr;
+  uint64_t* d_qseg = nullptr;
+  if (seg_count) {
+    d_seg = reinterpret_cast<uint64_t*>(w + lay.segs);
+    d_qseg = d_seg + seg_count + 1;
+  }
+  if (seg_count) {  // the sub-index table, staged in pinned memory owned by the handle
+    rc = ensure_segs(h, 2 * (static_cast<size_t>(seg_count) + 1));
+    if (rc) return rc;
+    std::memcpy(h->h_segs, seg_off, (seg_count + 1) * 8);
+    std::memcpy(h->h_segs + seg_count + 1, qseg_off, (seg_count + 1) * 8);
+  }
+  // everything the build puts on the stream, up to the read-back of status and counters; the
+  // per-stage events are left out of a captured graph (it is timed as a whole)
+  const bool use_graph = (p->flags & PG_FLAG_CUDA_GRAPH) && s != nullptr;
+  const bool stage_events = !use_graph;
+  auto enqueue = [&]() -> int {
+    if (seg_count) {
+      PG_CUDA(cudaMemcpyAsync(d_seg, h->h_segs, 2 * (seg_count + 1) * 8, cudaMemcpyHostToDevice,
+                              s));
+    }
 
-  PG_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(uint32_t), s));
-  PG_CUDA(cudaMemsetAsync(cnt, 0, C_COUNT * sizeof(unsigned long long), s));
-  PG_CUDA(cudaMemsetAsync(h->d_work, 0, 8 * sizeof(uint32_t), s));
-  PG_CUDA(cudaEventRecord(h->ev[0], s));
+    PG_CUDA(cudaMemsetAsync(h->d_status, 0, sizeof(uint32_t), s));
+    PG_CUDA(cudaMemsetAsync(cnt, 0, C_COUNT * sizeof(unsigned long long), s));
+    PG_CUDA(cudaMemsetAsync(h->d_work, 0, 8 * sizeof(uint32_t), s));
+    if (stage_events) PG_CUDA(cudaEventRecord(h->ev[0], s));
 
-  // K0 projection winners; K1+K2 phase-1 prune (rows read from gt through the winner)
-  PG_CUDA(pg::launch_match_winner(gt, q, p->gt_k, n, winner, h->d_status, sms, s));
-  PG_CUDA(cudaMemsetAsync(indeg, 0, n * 4, s));
-  pg::PruneArgs pa{};
-  pa.base = base;
-  pa.n = n;
-  pa.d = d;
-  pa.graph = nullptr;
-  pa.c = p->gt_k;
-  pa.gt = gt;
-  pa.winner = winner;
-  pa.gt_k = p->gt_k;
-  pa.p = p->proj_pruned;
-  pa.strict = 0;
-  pa.pruned = pruned;
-  pa.pruned_num = pnum;
-  pa.indeg = indeg;
-  pa.sorted = nullptr;
-  pa.evals = cnt + C_PROJ_PRUNE;
-  pa.status = h->d_status;
-  PG_CUDA(pg::launch_prune_reverse(pa, true, sms, s));
-  PG_CUDA(pg::launch_reverse_csr(pruned, pnum, p->proj_pruned, n, indeg, offs, tsum, cursor, edges,
-                                 sms, s));
-  PG_CUDA(pg::launch_reverse_lists(offs, edges, n, p->proj_reverse, rev, rnum, sms, s));
-  // K3 phase-1 merge -> projection graph
-  pg::MergeArgs ma{};
-  ma.base = base;
-  ma.n = n;
-  ma.d = d;
-  ma.pruned = pruned;
-  ma.pruned_num = pnum;
-  ma.p = p->proj_pruned;
-  ma.reverse = rev;
-  ma.reverse_num = rnum;
-  ma.r = p->proj_reverse;
-  ma.degree = p->proj_degree;
-  ma.strict = 0;
-  ma.out = proj;
-  ma.evals = cnt + C_PROJ_MERGE;
-  ma.status = h->d_status;
-  PG_CUDA(pg::launch_merge_prune(ma, sms, s));
-  PG_CUDA(cudaEventRecord(h->ev[1], s));
-
-  const uint32_t* g = proj;
-  uint32_t gdeg = p->proj_degree;
-  const uint32_t hslots = hash_slots_for(p->km, p->reset_iter, p->kp * p->kd);
-  for (uint32_t r = 0; r < p->link_rounds; r++) {
-    pg::SearchArgs sa{};
-    sa.base = base;
-    sa.n = n;
-    sa.d = d;
-    sa.graph = g;
-    sa.graph_degree = gdeg;
-    sa.km = p->km;
-    sa.kp = p->kp;
-    sa.kd = p->kd;
-    sa.reset_iter = p->reset_iter;
-    sa.seed_base = p->seed_base;
-    sa.max_iters = p->max_search_iters;
-    sa.order = nullptr;
-    sa.out = sres;
-    sa.evals = cnt + C_SEARCH + r;
-    sa.iters = cnt + C_ITERS + r;
-    sa.work = h->d_work + r;
-    sa.status = h->d_status;
-    sa.hash_slots = hslots;
-    PG_CUDA(pg::launch_search(sa, sms, h->smem_optin, s));
-    PG_CUDA(cudaEventRecord(h->ev[2 + 3 * r], s));
+    // K0 projection winners; K1+K2 phase-1 prune (rows read from gt through the winner)
+    PG_CUDA(pg::launch_match_winner(gt, q, p->gt_k, n, winner, h->d_status, sms, s, d_seg, d_qseg,
+                                    seg_count));
     PG_CUDA(cudaMemsetAsync(indeg, 0, n * 4, s));
-    pg::PruneArgs pr{};
-    pr.base = base;
-    pr.n = n;
-    pr.d = d;
-    pr.graph = sres;
-    pr.c = L;
-    pr.p = p->degree;
-    pr.strict = 1;
-    pr.pruned = pruned;
-    pr.pruned_num = pnum;
-    pr.indeg = indeg;
-    pr.sorted = nullptr;
-    pr.evals = cnt + C_PRUNE + r;
-    pr.status = h->d_status;
-    pr.rescored = cnt + C_RESCORED + r;
-    if (p->screen == PG_SCREEN_BF16 && pg::screen_supported(pr.c, d, pr.strict))
-      PG_CUDA(pg::launch_prune_screen(pr, sms, h->smem_optin, s));
-    else
-      PG_CUDA(pg::launch_prune_reverse(pr, false, sms, s));
-    PG_CUDA(pg::launch_reverse_csr(pruned, pnum, p->degree, n, indeg, offs, tsum, cursor, edges,
+    pg::PruneArgs pa{};
+    pa.base = base;
+    pa.n = n;
+    pa.d = d;
+    pa.graph = nullptr;
+    pa.c = p->gt_k;
+    pa.gt = gt;
+    pa.winner = winner;
+    pa.gt_k = p->gt_k;
+    pa.p = p->proj_pruned;
+    pa.strict = 0;
+    pa.pruned = pruned;
+    pa.pruned_num = pnum;
+    pa.indeg = indeg;
+    pa.sorted = nullptr;
+    pa.evals = cnt + C_PROJ_PRUNE;
+    pa.status = h->d_status;
+    pa.seg_off = d_seg;
+    pa.qseg_off = d_qseg;
+    pa.seg_count = seg_count;
+    PG_CUDA(pg::launch_prune_reverse(pa, true, sms, s));
+    PG_CUDA(pg::launch_reverse_csr(pruned, pnum, p->proj_pruned, n, indeg, offs, tsum, cursor, edges,
                                    sms, s));
-    PG_CUDA(pg::launch_reverse_lists(offs, edges, n, p->link_reverse, rev, rnum, sms, s));
-    PG_CUDA(cudaEventRecord(h->ev[3 + 3 * r], s));
-    pg::MergeArgs mr{};
-    mr.base = base;
-    mr.n = n;
-    mr.d = d;
-    mr.pruned = pruned;
-    mr.pruned_num = pnum;
-    mr.p = p->degree;
-    mr.reverse = rev;
-    mr.reverse_num = rnum;
-    mr.r = p->link_reverse;
-    mr.degree = p->degree;
-    mr.strict = 1;
-    mr.out = graph_out;
-    mr.evals = cnt + C_MERGE + r;
-    mr.status = h->d_status;
-    PG_CUDA(pg::launch_merge_prune(mr, sms, s));
-    PG_CUDA(cudaEventRecord(h->ev[4 + 3 * r], s));
-    g = graph_out;
-    gdeg = p->degree;
+    PG_CUDA(pg::launch_reverse_lists(offs, edges, n, p->proj_reverse, rev, rnum, sms, s));
+    // K3 phase-1 merge -> projection graph
+    pg::MergeArgs ma{};
+    ma.base = base;
+    ma.n = n;
+    ma.d = d;
+    ma.pruned = pruned;
+    ma.pruned_num = pnum;
+    ma.p = p->proj_pruned;
+    ma.reverse = rev;
+    ma.reverse_num = rnum;
+    ma.r = p->proj_reverse;
+    ma.degree = p->proj_degree;
+    ma.strict = 0;
+    ma.out = proj;
+    ma.evals = cnt + C_PROJ_MERGE;
+    ma.status = h->d_status;
+    PG_CUDA(pg::launch_merge_prune(ma, sms, s));
+    if (stage_events) PG_CUDA(cudaEventRecord(h->ev[1], s));
+
+    const uint32_t* g = proj;
+    uint32_t gdeg = p->proj_degree;
+    const uint32_t hslots = hash_slots_for(p->km, p->reset_iter, p->kp * p->kd);
+    for (uint32_t r = 0; r < p->link_rounds; r++) {
+      pg::SearchArgs sa{};
+      sa.base = base;
+      sa.n = n;
+      sa.d = d;
+      sa.graph = g;
+      sa.graph_degree = gdeg;
+      sa.km = p->km;
+      sa.kp = p->kp;
+      sa.kd = p->kd;
+      sa.reset_iter = p->reset_iter;
+      sa.seed_base = p->seed_base;
+      sa.max_iters = p->max_search_iters;
+      sa.order = nullptr;
+      sa.out = sres;
+      sa.evals = cnt + C_SEARCH + r;
+      sa.iters = cnt + C_ITERS + r;
+      sa.work = h->d_work + r;
+      sa.status = h->d_status;
+      sa.hash_slots = hslots;
+      sa.seg_off = d_seg;
+      sa.seg_count = seg_count;
+      PG_CUDA(pg::launch_search(sa, sms, h->smem_optin, s));
+      if (stage_events) PG_CUDA(cudaEventRecord(h->ev[2 + 3 * r], s));
+      PG_CUDA(cudaMemsetAsync(indeg, 0, n * 4, s));
+      pg::PruneArgs pr{};
+      pr.base = base;
+      pr.n = n;
+      pr.d = d;
+      pr.graph = sres;
+      pr.c = L;
+      pr.p = p->degree;
+      pr.strict = 1;
+      pr.pruned = pruned;
+      pr.pruned_num = pnum;
+      pr.indeg = indeg;
+      pr.sorted = nullptr;
+      pr.evals = cnt + C_PRUNE + r;
+      pr.status = h->d_status;
+      pr.rescored = cnt + C_RESCORED + r;
+      if (p->screen == PG_SCREEN_BF16 && pg::screen_supported(pr.c, d, pr.strict))
+        PG_CUDA(pg::launch_prune_screen(pr, sms, h->smem_optin, s));
+      else
+        PG_CUDA(pg::launch_prune_reverse(pr, false, sms, s));
+      PG_CUDA(pg::launch_reverse_csr(pruned, pnum, p->degree, n, indeg, offs, tsum, cursor, edges,
+                                     sms, s));
+      PG_CUDA(pg::launch_reverse_lists(offs, edges, n, p->link_reverse, rev, rnum, sms, s));
+      if (stage_events) PG_CUDA(cudaEventRecord(h->ev[3 + 3 * r], s));
+      pg::MergeArgs mr{};
+      mr.base = base;
+      mr.n = n;
+      mr.d = d;
+      mr.pruned = pruned;
+      mr.pruned_num = pnum;
+      mr.p = p->degree;
+      mr.reverse = rev;
+      mr.reverse_num = rnum;
+      mr.r = p->link_reverse;
+      mr.degree = p->degree;
+      mr.strict = 1;
+      mr.out = graph_out;
+      mr.evals = cnt + C_MERGE + r;
+      mr.status = h->d_status;
+      PG_CUDA(pg::launch_merge_prune(mr, sms, s));
+      if (stage_events) PG_CUDA(cudaEventRecord(h->ev[4 + 3 * r], s));
+      g = graph_out;
+      gdeg = p->degree;
+    }
+    if (p->link_rounds == 0 && graph_out) {
+      // no link rounds: the projection is the graph (degree columns, tomb padded)
+      PG_CUDA(cudaMemset2DAsync(graph_out, p->degree * 4, 0xFF, p->degree * 4, n, s));
+      PG_CUDA(cudaMemcpy2DAsync(graph_out, p->degree * 4, proj, p->proj_degree * 4,
+                                std::min(p->degree, p->proj_degree) * 4, n,
+                                cudaMemcpyDeviceToDevice, s));
+    }
+    if (seg_count) {  // global ids -> ids local to each sub-index
+      if (graph_out && p->link_rounds > 0)
+        PG_CUDA(pg::launch_localize(graph_out, n, p->degree, d_seg, seg_count, sms, s));
+      PG_CUDA(pg::launch_localize(proj, n, p->proj_degree, d_seg, seg_count, sms, s));
+    }
+    PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaMemcpyAsync(h->h_counters, cnt, C_COUNT * 8, cudaMemcpyDeviceToHost, s));
+    return PG_OK;
+  };
+  if (!use_graph) {
+    rc = enqueue();
+    if (rc) return rc;
+  } else {
+    GraphKey key;
+    key.p = *p;
+    key.ptrs[0] = base;
+    key.ptrs[1] = gt;
+    key.ptrs[2] = graph_out;
+    key.ptrs[3] = proj_out;
+    key.ptrs[4] = h->ws;
+    key.n = n;
+    key.q = q;
+    key.d = d;
+    key.segs.assign(h->h_segs ? h->h_segs : nullptr,
+                    h->h_segs ? h->h_segs + (seg_count ? 2 * (seg_count + 1) : 0) : nullptr);
+    if (!h->gexec || !(h->gkey == key)) {
+      if (h->gexec) cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+      cudaGraph_t graph = nullptr;
+      PG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      rc = enqueue();
+      cudaError_t ce = cudaStreamEndCapture(s, &graph);
+      if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+      }
+      if (ce != cudaSuccess) return fail(PG_ECUDA, "stream capture: %s", cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&h->gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) {
+        h->gexec = nullptr;
+        return fail(PG_ECUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+      }
+      h->gkey = key;
+    }
+    PG_CUDA(cudaEventRecord(h->ev[14], s));
+    PG_CUDA(cudaGraphLaunch(h->gexec, s));
+    PG_CUDA(cudaEventRecord(h->ev[15], s));
   }
-  if (p->link_rounds == 0 && graph_out) {
-    // no link rounds: the projection is the graph (degree columns, tomb padded)
-    PG_CUDA(cudaMemset2DAsync(graph_out, p->degree * 4, 0xFF, p->degree * 4, n, s));
-    PG_CUDA(cudaMemcpy2DAsync(graph_out, p->degree * 4, proj, p->proj_degree * 4,
-                              std::min(p->degree, p->proj_degree) * 4, n,
-                              cudaMemcpyDeviceToDevice, s));
-  }
-  PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, s));
-  PG_CUDA(cudaMemcpyAsync(h->h_counters, cnt, C_COUNT * 8, cudaMemcpyDeviceToHost, s));
   PG_CUDA(cudaStreamSynchronize(s));
   rc = status_to_error(*h->h_status);
   if (rc) return rc;
@@ -373,17 +486,19 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
       st->rescored[r] = c[C_RESCORED + r];
       st->evals_total += c[C_SEARCH + r] + c[C_PRUNE + r] + c[C_MERGE + r];
     }
-    float ms = 0;
-    cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
-    st->ms_proj = ms;
-    cudaEvent_t prev = h->ev[1];
-    for (uint32_t r = 0; r < p->link_rounds; r++) {
-      cudaEventElapsedTime(&st->ms_search[r], prev, h->ev[2 + 3 * r]);
-      cudaEventElapsedTime(&st->ms_prune[r], h->ev[2 + 3 * r], h->ev[3 + 3 * r]);
-      cudaEventElapsedTime(&st->ms_merge[r], h->ev[3 + 3 * r], h->ev[4 + 3 * r]);
-      prev = h->ev[4 + 3 * r];
+    if (use_graph) {  // one replay, timed as a whole
+      PG_CUDA(cudaEventElapsedTime(&st->ms_total, h->ev[14], h->ev[15]));
+    } else {
+      PG_CUDA(cudaEventElapsedTime(&st->ms_proj, h->ev[0], h->ev[1]));
+      cudaEvent_t prev = h->ev[1];
+      for (uint32_t r = 0; r < p->link_rounds; r++) {
+        PG_CUDA(cudaEventElapsedTime(&st->ms_search[r], prev, h->ev[2 + 3 * r]));
+        PG_CUDA(cudaEventElapsedTime(&st->ms_prune[r], h->ev[2 + 3 * r], h->ev[3 + 3 * r]));
+        PG_CUDA(cudaEventElapsedTime(&st->ms_merge[r], h->ev[3 + 3 * r], h->ev[4 + 3 * r]));
+        prev = h->ev[4 + 3 * r];
+      }
+      PG_CUDA(cudaEventElapsedTime(&st->ms_total, h->ev[0], prev));
     }
-    cudaEventElapsedTime(&st->ms_total, h->ev[0], prev);
   }
   return PG_OK;
 }
@@ -460,6 +575,8 @@ int pg_destroy(pg_handle h) {
   cudaFree(h->d_work);
   cudaFreeHost(h->h_status);
   cudaFreeHost(h->h_counters);
+  if (h->h_segs) cudaFreeHost(h->h_segs);
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
   for (int i = 0; i < 16; i++)
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);
   delete h;
@@ -550,6 +667,29 @@ int pg_build_host(pg_handle h, const pg_params* p, const float* base, uint64_t n
   cudaEventDestroy(t2);
   cudaEventDestroy(t3);
   return PG_OK;
+}
+
+int pg_build_batched_device(pg_handle h, const pg_params* p, const float* d_base, uint32_t d,
+                            const uint32_t* d_gt, const uint64_t* node_off,
+                            const uint64_t* query_off, uint32_t count, uint32_t* d_graph,
+                            uint32_t* d_proj, pg_stats* st) {
+  if (!h) return fail(PG_EINVAL, "handle is NULL");
+  if (!node_off || !query_off || count == 0) return fail(PG_EINVAL, "empty sub-index table");
+  if (node_off[0] != 0 || query_off[0] != 0) return fail(PG_EINVAL, "offsets must start at 0");
+  for (uint32_t i = 0; i < count; i++) {
+    if (node_off[i + 1] <= node_off[i]) return fail(PG_EINVAL, "sub-index %u is empty", i);
+    if (query_off[i + 1] < query_off[i]) return fail(PG_EINVAL, "query offsets must ascend");
+  }
+  const uint64_t n = node_off[count], q = query_off[count];
+  int rc = check_params(p, n, d, q);
+  if (rc) return rc;
+  if (!d_base || !d_gt || (p->link_rounds > 0 && !d_graph))
+    return fail(PG_EINVAL, "base, gt and graph must be device pointers");
+  if (!aligned16(d_base)) return fail(PG_EINVAL, "base must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  if (st) std::memset(st, 0, sizeof(*st));
+  return run_build(h, p, d_base, n, d, d_gt, q, d_graph, d_proj, st, node_off, query_off, count);
 }
 
 // ---------------------------------------------------------------- stage entry points

@@ -178,4 +178,16 @@ __device__ __forceinline__ void raise_error(uint32_t* status, uint32_t code) {
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
+// Sub-index of global id x in a batched build: the last s with off[s] <= x (off has count + 1
+// ascending entries, off[0] = 0).  count == 0 means a single index.
+__device__ __forceinline__ uint32_t segment_of(const uint64_t* off, uint32_t count, uint64_t x) {
+  if (count == 0) return 0;
+  uint32_t lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 }  // namespace pg

@@ -30,16 +30,25 @@ __device__ __forceinline__ uint32_t winner_query(uint32_t key) {
 }
 
 __global__ void k_match_winner(const uint32_t* __restrict__ gt, uint64_t q, uint32_t gt_k,
-                               uint64_t n, uint32_t* __restrict__ winner, uint32_t* status) {
+                               uint64_t n, uint32_t* __restrict__ winner, uint32_t* status,
+                               const uint64_t* __restrict__ seg_off,
+                               const uint64_t* __restrict__ qseg_off, uint32_t seg_count) {
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
   for (uint64_t qi = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; qi < q;
        qi += stride) {
-    const uint32_t b = gt[qi * gt_k];
-    if (b == kTomb) continue;
-    if (b >= n) {
+    uint64_t off = 0, ns = n;  // the query's sub-index: its ground-truth ids are local to it
+    if (seg_count) {
+      const uint32_t sg = segment_of(qseg_off, seg_count, qi);
+      off = seg_off[sg];
+      ns = seg_off[sg + 1] - off;
+    }
+    const uint32_t bl = gt[qi * gt_k];
+    if (bl == kTomb) continue;
+    if (bl >= ns) {
       raise_error(status, kErrBadId);
       continue;
     }
+    const uint64_t b = bl + off;
     const bool real = gt[qi * gt_k + 1] != kTomb;
     atomicMin(winner + b, winner_key(static_cast<uint32_t>(qi), real));
   }
@@ -154,7 +163,15 @@ __global__ void __launch_bounds__(256) k_prune_reverse(PruneArgs a) {
     uint32_t id[E];
     bool valid[E];
     uint32_t w = kTomb;
-    if (PHASE1) w = winner_query(a.winner[b]);
+    uint64_t goff = 0, gn = a.n;  // phase 1: ground-truth ids are local to b's sub-index
+    if (PHASE1) {
+      w = winner_query(a.winner[b]);
+      if (a.seg_count) {
+        const uint32_t sg = segment_of(a.seg_off, a.seg_count, b);
+        goff = a.seg_off[sg];
+        gn = a.seg_off[sg + 1] - goff;
+      }
+    }
     if (PHASE1 && w == kTomb) {  // nobody's top-1: an all-tomb row, nothing kept
       if (lane == 0) a.pruned_num[b] = 0;
       if (a.sorted)
@@ -166,10 +183,19 @@ __global__ void __launch_bounds__(256) k_prune_reverse(PruneArgs a) {
       const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
       uint32_t x = kTomb;
       if (j < a.c) {
-        if (PHASE1)
+        if (PHASE1) {
           x = (j + 2 < a.gt_k) ? a.gt[static_cast<uint64_t>(w) * a.gt_k + j + 1] : kTomb;
-        else
+          if (x != kTomb) {
+            if (x >= gn) {  // out-of-range input id
+              raise_error(a.status, kErrBadId);
+              x = kTomb;
+            } else {
+              x = static_cast<uint32_t>(x + goff);
+            }
+          }
+        } else {
           x = a.graph[b * a.c + j];
+        }
       }
       if (x >= a.n && x != kTomb && x != kMaskedTomb) {  // out-of-range input id
         raise_error(a.status, kErrBadId);
@@ -517,11 +543,29 @@ static int grid_for(uint64_t items, int per_block, int num_sms, int max_per_sm) 
 }
 
 cudaError_t launch_match_winner(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint64_t n,
-                                uint32_t* winner, uint32_t* status, int num_sms,
-                                cudaStream_t st) {
+                                uint32_t* winner, uint32_t* status, int num_sms, cudaStream_t st,
+                                const uint64_t* seg_off, const uint64_t* qseg_off,
+                                uint32_t seg_count) {
   cudaError_t e = cudaMemsetAsync(winner, 0xFF, n * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  k_match_winner<<<grid_for(q, 256, num_sms, 8), 256, 0, st>>>(gt, q, gt_k, n, winner, status);
+  k_match_winner<<<grid_for(q, 256, num_sms, 8), 256, 0, st>>>(gt, q, gt_k, n, winner, status,
+                                                               seg_off, qseg_off, seg_count);
+  return cudaGetLastError();
+}
+
+__global__ void k_localize(uint32_t* __restrict__ rows, uint64_t n, uint32_t deg,
+                           const uint64_t* __restrict__ seg_off, uint32_t seg_count) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n * deg;
+       i += stride) {
+    const uint32_t v = rows[i];
+    if (v != kTomb) rows[i] = static_cast<uint32_t>(v - seg_off[segment_of(seg_off, seg_count, i / deg)]);
+  }
+}
+
+cudaError_t launch_localize(uint32_t* rows, uint64_t n, uint32_t deg, const uint64_t* seg_off,
+                            uint32_t seg_count, int num_sms, cudaStream_t st) {
+  k_localize<<<grid_for(n * deg, 256, num_sms, 8), 256, 0, st>>>(rows, n, deg, seg_off, seg_count);
   return cudaGetLastError();
 }
 

@@ -23,6 +23,11 @@ struct PruneArgs {
   unsigned long long* evals;
   uint32_t* status;        // error flags (kErr*)
   unsigned long long* rescored;  // screened kernel: occlusion tests re-scored exactly (nullable)
+  // batched builds: node-id offsets of the sub-indexes (seg_count + 1 entries, device) and the
+  // query offsets of their ground-truth rows; seg_count == 0 means one index of n nodes
+  const uint64_t* seg_off;
+  const uint64_t* qseg_off;
+  uint32_t seg_count;
 };
 
 struct MergeArgs {
@@ -57,10 +62,17 @@ struct SearchArgs {
   uint32_t* work;         // work counter, zeroed before the launch
   uint32_t* status;
   uint32_t hash_slots;    // visited-set capacity per warp (power of two)
+  const uint64_t* seg_off;  // batched builds: sub-index node offsets (seg_count + 1), else NULL
+  uint32_t seg_count;
 };
 
 cudaError_t launch_match_winner(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint64_t n,
-                                uint32_t* winner, uint32_t* status, int num_sms, cudaStream_t st);
+                                uint32_t* winner, uint32_t* status, int num_sms, cudaStream_t st,
+                                const uint64_t* seg_off = nullptr,
+                                const uint64_t* qseg_off = nullptr, uint32_t seg_count = 0);
+// Rewrites global ids of a batched build's rows (n x deg) to ids local to each row's sub-index.
+cudaError_t launch_localize(uint32_t* rows, uint64_t n, uint32_t deg, const uint64_t* seg_off,
+                            uint32_t seg_count, int num_sms, cudaStream_t st);
 cudaError_t launch_match_rows(const uint32_t* gt, uint32_t gt_k, uint64_t n,
                               const uint32_t* winner, uint32_t* out, int num_sms,
                               cudaStream_t st);

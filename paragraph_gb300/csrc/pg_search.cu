@@ -248,7 +248,14 @@ __global__ void __launch_bounds__(32) k_search(SearchArgs a) {
 
     // seeds: every slot is scored (Gsearcher.cuh:958-976 has no visited test)
     {
-      const uint32_t node = static_cast<uint32_t>((a.seed_base + static_cast<uint64_t>(lane)) % a.n);
+      uint64_t soff = 0, sn = a.n;  // entry points are drawn inside the query's sub-index
+      if (a.seg_count) {
+        const uint32_t sg = segment_of(a.seg_off, a.seg_count, qid);
+        soff = a.seg_off[sg];
+        sn = a.seg_off[sg + 1] - soff;
+      }
+      const uint32_t node =
+          static_cast<uint32_t>((a.seed_base + static_cast<uint64_t>(lane)) % sn + soff);
       const float dist = stage_and_score<KSTEPS>(a, q, node, true, rows, mbar, phase, ok);
       if (!ok) break;
       key[KM_S] = pack_key(dist, km + lane);
@@ -484,7 +491,7 @@ __device__ __forceinline__ float score_passes(const SearchArgs& a, const Q4<KSTE
 }  // namespace
 
 template <int KSTEPS, int ROWS>
-__global__ void __launch_bounds__(32, 20) k_search_m32(SearchArgs a) {
+__global__ void __launch_bounds__(32, KSTEPS <= 8 ? 20 : 12) k_search_m32(SearchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const uint32_t lane = lane_id();
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw);
@@ -524,7 +531,14 @@ __global__ void __launch_bounds__(32, 20) k_search_m32(SearchArgs a) {
     uint64_t cand_key;
     uint32_t cand_id;
     {  // seeds: every slot is scored (Gsearcher.cuh:958-976 has no visited test)
-      const uint32_t node = static_cast<uint32_t>((a.seed_base + static_cast<uint64_t>(lane)) % a.n);
+      uint64_t soff = 0, sn = a.n;  // entry points are drawn inside the query's sub-index
+      if (a.seg_count) {
+        const uint32_t sg = segment_of(a.seg_off, a.seg_count, qid);
+        soff = a.seg_off[sg];
+        sn = a.seg_off[sg + 1] - soff;
+      }
+      const uint32_t node =
+          static_cast<uint32_t>((a.seed_base + static_cast<uint64_t>(lane)) % sn + soff);
       const float dist = score_passes<KSTEPS, ROWS>(a, q, node, true, rows, mbar, phase, ok);
       if (!ok) break;
       cand_key = pack_key(dist, 32u + lane);
