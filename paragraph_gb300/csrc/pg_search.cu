@@ -722,6 +722,7 @@ cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, c
   const bool small = a.d <= 256;
   switch (km_s) {
     case 1:
+      if (a.d <= 224) return launch_search_m32<7>(a, num_sms, smem_optin, st);
       return small ? launch_search_m32<8>(a, num_sms, smem_optin, st)
                    : launch_search_m32<16>(a, num_sms, smem_optin, st);
     case 2:
