@@ -1,6 +1,7 @@
 // pg_screen.cu -- screened prune + reverse (K6/K10) with a BF16 tensor-core Gram.
 //
-// Same result as k_prune_reverse (strict rounds), bit for bit.  Per node (one warp):
+// Same result as k_prune_reverse (strict rounds), bit for bit.  Per node (one warp, up to 64
+// candidates):
 //   1. one pass over the candidate rows: each lane runs the exact FP32 chain dist(b, c) for its
 //      candidates (distance_between's order, Gbuilder.cuh:785-797) and, from the same loads,
 //      rounds the row to BF16 and accumulates two norms per row, |x| and |x - bf16(x)|;
@@ -68,8 +69,197 @@ __host__ __device__ inline uint32_t screen_dp(uint32_t d) { return (d + 15u) / 1
 
 }  // namespace
 
+namespace {
+
 constexpr uint32_t kChunkStride = 24;  // BF16 per chunk row: 48 B keeps ldmatrix rows conflict-free
 constexpr uint32_t kTri = kScrC * (kScrC - 1) / 2;  // packed strictly-lower Gram entries
+
+// Per-warp shared memory of the screened kernels.
+struct ScreenSmem {
+  __nv_bfloat16* chunk;  // kScrC x kChunkStride: one K chunk of the BF16 rows
+  float* G;              // kTri: packed strictly-lower Gram
+  uint32_t* ids;         // sorted ids
+  float* dist;           // sorted exact distances to the node
+  float* nrm;            // |x| per original slot
+  float* err;            // |x - bf16(x)| per original slot
+  uint32_t* orig;        // sorted position -> original slot
+  uint32_t* kept_o;      // kept entries: original slot
+  uint32_t* kept_i;      // kept entries: id
+};
+
+__device__ __forceinline__ ScreenSmem screen_smem(unsigned char* raw) {
+  ScreenSmem m;
+  m.chunk = reinterpret_cast<__nv_bfloat16*>(raw);
+  m.G = reinterpret_cast<float*>(raw + static_cast<size_t>(kScrC) * kChunkStride * 2);
+  m.ids = reinterpret_cast<uint32_t*>(m.G + kTri);
+  m.dist = reinterpret_cast<float*>(m.ids + kScrC);
+  m.nrm = m.dist + kScrC;
+  m.err = m.nrm + kScrC;
+  m.orig = reinterpret_cast<uint32_t*>(m.err + kScrC);
+  m.kept_o = m.orig + kScrC;
+  m.kept_i = m.kept_o + kScrC;
+  return m;
+}
+
+__device__ __forceinline__ uint32_t tri_index(uint32_t r, uint32_t c) {  // r > c
+  return r * (r - 1) / 2 + c;
+}
+
+// Steps 1 and 2 for one node: exact chains dist(b, id[s]) (FLT_MAX where !valid[s]), BF16
+// rounding, norms, and the streamed tensor-core Gram of the 64 slots into sm.G / sm.nrm / sm.err.
+// Lane l owns slots l and 32 + l.
+__device__ __forceinline__ void screen_rows_and_gram(const float* __restrict__ base, uint32_t d,
+                                                     const float* __restrict__ brow,
+                                                     const uint32_t (&id)[2],
+                                                     const bool (&valid)[2], const ScreenSmem& sm,
+                                                     float (&dist)[2]) {
+  const uint32_t lane = lane_id();
+  const uint32_t dp = screen_dp(d);
+  const uint32_t g = lane >> 2, t4 = lane & 3u;
+  const float4* b4 = reinterpret_cast<const float4*>(brow);
+  const float4* r4[2];
+#pragma unroll
+  for (int s = 0; s < 2; s++)
+    r4[s] = reinterpret_cast<const float4*>(valid[s] ? base + static_cast<uint64_t>(id[s]) * d
+                                                     : brow);
+  float acc[2] = {0.f, 0.f}, nn[2] = {0.f, 0.f}, ee[2] = {0.f, 0.f};
+  float gm[20][4];  // lower-triangle m16n8 tiles: tile (mt, nt) at mt*(mt+1) + nt, nt <= 2mt+1
+#pragma unroll
+  for (int i = 0; i < 20; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) gm[i][j] = 0.f;
+  const uint32_t n4 = d >> 2;
+  for (uint32_t k0 = 0; k0 < dp; k0 += 16) {
+#pragma unroll
+    for (uint32_t q = 0; q < 4; q++) {
+      const uint32_t i = (k0 >> 2) + q;  // float4 index
+      const bool in = i < n4;
+      const float4 u = in ? __ldg(b4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        const float4 v = in ? __ldg(r4[s] + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        uint2 packed = make_uint2(0u, 0u);
+        if (in) {
+          acc[s] = fmaf(u.x, v.x, acc[s]);
+          acc[s] = fmaf(u.y, v.y, acc[s]);
+          acc[s] = fmaf(u.z, v.z, acc[s]);
+          acc[s] = fmaf(u.w, v.w, acc[s]);
+          float e0, e1, e2, e3;
+          packed.x = bf16x2_bits(v.x, v.y, e0, e1);
+          packed.y = bf16x2_bits(v.z, v.w, e2, e3);
+          nn[s] = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, nn[s]))));
+          ee[s] = fmaf(e0, e0, fmaf(e1, e1, fmaf(e2, e2, fmaf(e3, e3, ee[s]))));
+        }
+        const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+        *reinterpret_cast<uint2*>(sm.chunk + j * kChunkStride + 4 * q) =
+            valid[s] ? packed : make_uint2(0u, 0u);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int mt = 0; mt < 4; mt++) {
+      uint32_t af[4];
+      ldsm_x4(af, sm.chunk + (16 * mt + (lane & 15u)) * kChunkStride + (lane >> 4) * 8);
+#pragma unroll
+      for (int nt = 0; nt <= 2 * mt + 1; nt++) {
+        uint32_t bf[2];
+        ldsm_x2(bf, sm.chunk + (8 * nt + (lane & 7u)) * kChunkStride + ((lane >> 3) & 1u) * 8);
+        mma_bf16(gm[mt * (mt + 1) + nt], af, bf);
+      }
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int mt = 0; mt < 4; mt++)
+#pragma unroll
+    for (int nt = 0; nt <= 2 * mt + 1; nt++) {
+      const float* c = gm[mt * (mt + 1) + nt];
+      const uint32_t r0 = 16 * mt + g, c0 = 8 * nt + 2 * t4;
+      if (r0 > c0) sm.G[tri_index(r0, c0)] = c[0];
+      if (r0 > c0 + 1) sm.G[tri_index(r0, c0 + 1)] = c[1];
+      if (r0 + 8 > c0) sm.G[tri_index(r0 + 8, c0)] = c[2];
+      if (r0 + 8 > c0 + 1) sm.G[tri_index(r0 + 8, c0 + 1)] = c[3];
+    }
+#pragma unroll
+  for (int s = 0; s < 2; s++) {
+    const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+    sm.nrm[j] = valid[s] ? sqrtf(nn[s]) * 1.0001f : 0.f;
+    sm.err[j] = valid[s] ? sqrtf(ee[s]) * 1.0001f : 0.f;
+    dist[s] = valid[s] ? -acc[s] : FLT_MAX;
+  }
+}
+
+// Sorts the 64 slots by (exact distance, slot) into sm.ids / sm.dist / sm.orig (first c).
+__device__ __forceinline__ void screen_sort(uint32_t (&id)[2], const float (&dist)[2], uint32_t c,
+                                            const ScreenSmem& sm) {
+  const uint32_t lane = lane_id();
+  uint64_t key[2];
+#pragma unroll
+  for (int s = 0; s < 2; s++) {
+    const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+    key[s] = (j < c) ? pack_key(dist[s], j) : ~0ull;
+  }
+  warp_sort_kv<2>(key, id);
+#pragma unroll
+  for (int s = 0; s < 2; s++) {
+    const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
+    if (i < c) {
+      sm.ids[i] = id[s];
+      sm.dist[i] = key_to_dist(key[s]);
+      sm.orig[i] = key_pos(key[s]);
+    }
+  }
+  __syncwarp();
+}
+
+// Occlusion test of sorted entry j against kept[0..k] (Gbuilder.cuh:1163-1181):
+// decided from the screened Gram outside the error bound, re-scored with the exact chain inside
+// it.  *checks gets the reference's comparison count, *resc the number of exact re-scores.
+__device__ __forceinline__ bool screen_occluded(const float* __restrict__ base, uint32_t d,
+                                                float c_acc, float c_seq, const ScreenSmem& sm,
+                                                uint32_t j, uint32_t k, uint64_t* checks,
+                                                uint64_t* resc) {
+  const uint32_t lane = lane_id();
+  const uint32_t p = sm.ids[j];
+  const float dpj = sm.dist[j];
+  const uint32_t po = sm.orig[j];
+  const float np = sm.nrm[po], ep = sm.err[po];
+  for (uint32_t t0 = 0; t0 <= k; t0 += 32) {
+    const uint32_t t = t0 + lane;
+    bool yes = false, amb = false;
+    if (t <= k) {
+      const uint32_t ro = sm.kept_o[t];
+      const float nr = sm.nrm[ro], er = sm.err[ro];
+      const float dhat = -sm.G[po > ro ? tri_index(po, ro) : tri_index(ro, po)];
+      const float bound = ep * (nr + er) + np * er + c_acc * (np + ep) * (nr + er) +
+                          c_seq * np * nr + fabsf(dhat) * 9.5367431640625e-07f + 1e-30f;
+      if (dhat + bound < dpj)
+        yes = true;
+      else if (!(dhat - bound >= dpj))
+        amb = true;
+    }
+    unsigned m_yes = __ballot_sync(kFull, yes);
+    const unsigned m_amb = __ballot_sync(kFull, amb);
+    const unsigned before = m_yes ? ((m_yes & (0u - m_yes)) - 1u) : 0xFFFFFFFFu;
+    const unsigned need = m_amb & before;
+    if (need) {
+      bool ex = false;
+      if ((need >> lane) & 1u)
+        ex = dist_seq(base + static_cast<uint64_t>(p) * d,
+                      base + static_cast<uint64_t>(sm.kept_i[t]) * d, d) < dpj;
+      m_yes |= __ballot_sync(kFull, ex);
+      *resc += (lane == 0) ? __popc(need) : 0u;
+    }
+    if (m_yes) {
+      *checks += static_cast<uint32_t>(__ffs(static_cast<int>(m_yes)));
+      return true;
+    }
+    *checks += min(32u, k + 1 - t0);
+  }
+  return false;
+}
+
+}  // namespace
 
 // bytes of shared memory per warp
 size_t screen_smem_per_warp(uint32_t /*d*/) {
@@ -82,31 +272,15 @@ bool screen_supported(uint32_t c, uint32_t d, int strict) {
   return strict && c <= static_cast<uint32_t>(kScrC) && d >= 4 && d <= 1024 && (d % 4) == 0;
 }
 
-__device__ __forceinline__ uint32_t tri_index(uint32_t r, uint32_t c) {  // r > c
-  return r * (r - 1) / 2 + c;
-}
-
 __global__ void __launch_bounds__(32, 16) k_prune_screen(PruneArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const ScreenSmem sm = screen_smem(smem_raw);
   const uint32_t lane = lane_id();
   const uint32_t d = a.d;
-  const uint32_t dp = screen_dp(d);
-  __nv_bfloat16* Ck = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-  float* G = reinterpret_cast<float*>(smem_raw + static_cast<size_t>(kScrC) * kChunkStride * 2);
-  uint32_t* ids_s = reinterpret_cast<uint32_t*>(G + kTri);
-  float* dist_s = reinterpret_cast<float*>(ids_s + kScrC);
-  float* nrm_s = dist_s + kScrC;   // |x| per original candidate slot
-  float* err_s = nrm_s + kScrC;    // |x - bf16(x)|
-  uint32_t* orig_s = reinterpret_cast<uint32_t*>(err_s + kScrC);  // sorted -> original slot
-  uint32_t* kept_o = orig_s + kScrC;  // kept: original slot
-  uint32_t* kept_i = kept_o + kScrC;  // kept: id
-  const float c_acc = static_cast<float>(dp + 32) * 4.76837158e-07f;  // 2^-21
-  const float c_seq = static_cast<float>(d + 2) * 1.19209290e-07f;    // 2^-23
-  const uint32_t g = lane >> 2, t4 = lane & 3u;
+  const float c_acc = static_cast<float>(screen_dp(d) + 32) * 4.76837158e-07f;  // 2^-21
+  const float c_seq = static_cast<float>(d + 2) * 1.19209290e-07f;              // 2^-23
   uint64_t ev = 0, resc = 0;
-
   for (uint64_t b = blockIdx.x; b < a.n; b += gridDim.x) {
-    const float* brow = a.base + b * d;
     uint32_t id[2];
     bool valid[2];
 #pragma unroll
@@ -120,162 +294,34 @@ __global__ void __launch_bounds__(32, 16) k_prune_screen(PruneArgs a) {
       id[s] = x;
       valid[s] = (x != kTomb && x != static_cast<uint32_t>(b) && x != kMaskedTomb);
     }
-    const float4* b4 = reinterpret_cast<const float4*>(brow);
-    const float4* r4[2];
-#pragma unroll
-    for (int s = 0; s < 2; s++)
-      r4[s] = reinterpret_cast<const float4*>(valid[s] ? a.base + static_cast<uint64_t>(id[s]) * d
-                                                       : brow);
-    float acc[2] = {0.f, 0.f}, nn[2] = {0.f, 0.f}, ee[2] = {0.f, 0.f};
-    float gm[20][4];  // lower-triangle m16n8 tiles: tile (mt, nt) at mt*(mt+1) + nt, nt <= 2mt+1
-#pragma unroll
-    for (int i = 0; i < 20; i++)
-#pragma unroll
-      for (int j = 0; j < 4; j++) gm[i][j] = 0.f;
-    const uint32_t n4 = d >> 2;
-    // ---- 1+2. stream K in chunks of 16: exact chains, BF16 chunk, MMA on the chunk
-    for (uint32_t k0 = 0; k0 < dp; k0 += 16) {
-#pragma unroll
-      for (uint32_t q = 0; q < 4; q++) {
-        const uint32_t i = (k0 >> 2) + q;  // float4 index
-        const bool in = i < n4;
-        const float4 u = in ? __ldg(b4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-        for (int s = 0; s < 2; s++) {
-          const float4 v = in ? __ldg(r4[s] + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-          uint2 packed = make_uint2(0u, 0u);
-          if (in) {
-            acc[s] = fmaf(u.x, v.x, acc[s]);
-            acc[s] = fmaf(u.y, v.y, acc[s]);
-            acc[s] = fmaf(u.z, v.z, acc[s]);
-            acc[s] = fmaf(u.w, v.w, acc[s]);
-            float e0, e1, e2, e3;
-            packed.x = bf16x2_bits(v.x, v.y, e0, e1);
-            packed.y = bf16x2_bits(v.z, v.w, e2, e3);
-            nn[s] = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, nn[s]))));
-            ee[s] = fmaf(e0, e0, fmaf(e1, e1, fmaf(e2, e2, fmaf(e3, e3, ee[s]))));
-          }
-          const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
-          *reinterpret_cast<uint2*>(Ck + j * kChunkStride + 4 * q) =
-              valid[s] ? packed : make_uint2(0u, 0u);
-        }
-      }
-      __syncwarp();
-#pragma unroll
-      for (int mt = 0; mt < 4; mt++) {
-        uint32_t af[4];
-        ldsm_x4(af, Ck + (16 * mt + (lane & 15u)) * kChunkStride + (lane >> 4) * 8);
-#pragma unroll
-        for (int nt = 0; nt <= 2 * mt + 1; nt++) {
-          uint32_t bf[2];
-          ldsm_x2(bf, Ck + (8 * nt + (lane & 7u)) * kChunkStride + ((lane >> 3) & 1u) * 8);
-          mma_bf16(gm[mt * (mt + 1) + nt], af, bf);
-        }
-      }
-      __syncwarp();
-    }
-#pragma unroll
-    for (int mt = 0; mt < 4; mt++)
-#pragma unroll
-      for (int nt = 0; nt <= 2 * mt + 1; nt++) {
-        const float* c = gm[mt * (mt + 1) + nt];
-        const uint32_t r0 = 16 * mt + g, c0 = 8 * nt + 2 * t4;
-        if (r0 > c0) G[tri_index(r0, c0)] = c[0];
-        if (r0 > c0 + 1) G[tri_index(r0, c0 + 1)] = c[1];
-        if (r0 + 8 > c0) G[tri_index(r0 + 8, c0)] = c[2];
-        if (r0 + 8 > c0 + 1) G[tri_index(r0 + 8, c0 + 1)] = c[3];
-      }
-#pragma unroll
-    for (int s = 0; s < 2; s++) {
-      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
-      nrm_s[j] = valid[s] ? sqrtf(nn[s]) * 1.0001f : 0.f;
-      err_s[j] = valid[s] ? sqrtf(ee[s]) * 1.0001f : 0.f;
-    }
     float dist[2];
-#pragma unroll
-    for (int s = 0; s < 2; s++) dist[s] = valid[s] ? -acc[s] : FLT_MAX;
+    screen_rows_and_gram(a.base, d, a.base + b * d, id, valid, sm, dist);
     const unsigned v0 = __ballot_sync(kFull, valid[0]);  // every lane takes part
     const unsigned v1 = __ballot_sync(kFull, valid[1]);
     ev += (lane == 0) ? (__popc(v0) + __popc(v1)) : 0u;
+    screen_sort(id, dist, a.c, sm);
 
-    // ---- sort by (exact distance, slot): the stable order of bubble_sort
-    uint64_t key[2];
-#pragma unroll
-    for (int s = 0; s < 2; s++) {
-      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
-      key[s] = (j < a.c) ? pack_key(dist[s], j) : ~0ull;
-    }
-    warp_sort_kv<2>(key, id);
-#pragma unroll
-    for (int s = 0; s < 2; s++) {
-      const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
-      if (i < a.c) {
-        ids_s[i] = id[s];
-        dist_s[i] = key_to_dist(key[s]);
-        orig_s[i] = key_pos(key[s]);
-      }
-    }
-    __syncwarp();
-
-    // ---- 3. screened RNG scan
-    const uint32_t first = ids_s[0];
+    const uint32_t first = sm.ids[0];
     if (first == kTomb || first == kMaskedTomb) {
       if (lane == 0) a.pruned_num[b] = 0;
       __syncwarp();
       continue;
     }
     if (lane == 0) {
-      kept_o[0] = orig_s[0];
-      kept_i[0] = first;
+      sm.kept_o[0] = sm.orig[0];
+      sm.kept_i[0] = first;
     }
     __syncwarp();
     uint32_t k = 0;
     uint64_t checks = 0;
     for (uint32_t j = 1; j < a.c; j++) {
-      const uint32_t p = ids_s[j];
+      const uint32_t p = sm.ids[j];
       if (p == kTomb || p == kMaskedTomb) break;
-      const float dpj = dist_s[j];
-      const uint32_t po = orig_s[j];
-      const float np = nrm_s[po], ep = err_s[po];
-      bool occ = false;
-      for (uint32_t t0 = 0; t0 <= k; t0 += 32) {
-        const uint32_t t = t0 + lane;
-        bool yes = false, amb = false;
-        if (t <= k) {
-          const uint32_t ro = kept_o[t];
-          const float nr = nrm_s[ro], er = err_s[ro];
-          const float dhat = -G[po > ro ? tri_index(po, ro) : tri_index(ro, po)];
-          const float bound = ep * (nr + er) + np * er + c_acc * (np + ep) * (nr + er) +
-                              c_seq * np * nr + fabsf(dhat) * 9.5367431640625e-07f + 1e-30f;
-          if (dhat + bound < dpj)
-            yes = true;
-          else if (!(dhat - bound >= dpj))
-            amb = true;
-        }
-        unsigned m_yes = __ballot_sync(kFull, yes);
-        const unsigned m_amb = __ballot_sync(kFull, amb);
-        const unsigned before = m_yes ? ((m_yes & (0u - m_yes)) - 1u) : 0xFFFFFFFFu;
-        const unsigned need = m_amb & before;
-        if (need) {
-          bool ex = false;
-          if ((need >> lane) & 1u)
-            ex = dist_seq(a.base + static_cast<uint64_t>(p) * d,
-                          a.base + static_cast<uint64_t>(kept_i[t]) * d, d) < dpj;
-          m_yes |= __ballot_sync(kFull, ex);
-          resc += (lane == 0) ? __popc(need) : 0u;
-        }
-        if (m_yes) {
-          checks += static_cast<uint32_t>(__ffs(static_cast<int>(m_yes)));
-          occ = true;
-          break;
-        }
-        checks += min(32u, k + 1 - t0);
-      }
-      if (!occ) {
+      if (!screen_occluded(a.base, d, c_acc, c_seq, sm, j, k, &checks, &resc)) {
         k++;
         if (lane == 0) {
-          kept_o[k] = po;
-          kept_i[k] = p;
+          sm.kept_o[k] = sm.orig[j];
+          sm.kept_i[k] = p;
         }
         __syncwarp();
         if (k == a.p - 1) break;
@@ -285,7 +331,7 @@ __global__ void __launch_bounds__(32, 16) k_prune_screen(PruneArgs a) {
     const uint32_t cnt = k + 1;
     if (lane == 0) a.pruned_num[b] = cnt;
     for (uint32_t t = lane; t < cnt; t += 32) {
-      const uint32_t dst = kept_i[t];
+      const uint32_t dst = sm.kept_i[t];
       a.pruned[b * a.p + t] = dst;
       atomicAdd(a.indeg + dst, 1u);
     }
@@ -297,27 +343,36 @@ __global__ void __launch_bounds__(32, 16) k_prune_screen(PruneArgs a) {
   }
 }
 
-cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_optin,
-                                cudaStream_t st) {
-  if (!screen_supported(a.c, a.d, a.strict)) return cudaErrorInvalidValue;
-  const size_t smem = screen_smem_per_warp(a.d);
+template <typename Args>
+static cudaError_t launch_screen_kernel(void (*kern)(Args), const Args& a, uint64_t n,
+                                        uint32_t d, int num_sms, size_t smem_optin,
+                                        cudaStream_t st) {
+  const size_t smem = screen_smem_per_warp(d);
   if (smem > smem_optin) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(k_prune_screen, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
   if (e != cudaSuccess) return e;
   // Hub rows recur across many nodes' candidate lists, so L1 hits matter more than resident
   // warps: keep about a quarter of the unified L1/shared capacity as L1 (measured on GB300 at
-  // 1M x 200: 22 ms per round with this split against 35 ms with the largest shared carveout).
-  e = cudaFuncSetAttribute(k_prune_screen, cudaFuncAttributePreferredSharedMemoryCarveout, 76);
+  // 1M x 200: 22 ms per prune round with this split against 35 ms with the largest shared
+  // carveout).  A screened merge (K7/K11) built the same way was slower than the plain merge at
+  // every list-length split tried: most merged lists hold 32 entries or fewer.
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 76);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_prune_screen, 32, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   uint64_t blocks = static_cast<uint64_t>(num_sms) * per_sm;
-  if (blocks > a.n) blocks = a.n;
-  k_prune_screen<<<static_cast<unsigned>(blocks), 32, smem, st>>>(a);
+  if (blocks > n) blocks = n;
+  kern<<<static_cast<unsigned>(blocks), 32, smem, st>>>(a);
   return cudaGetLastError();
+}
+
+cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_optin,
+                                cudaStream_t st) {
+  if (!screen_supported(a.c, a.d, a.strict)) return cudaErrorInvalidValue;
+  return launch_screen_kernel(k_prune_screen, a, a.n, a.d, num_sms, smem_optin, st);
 }
 
 }  // namespace pg
