@@ -11,7 +11,7 @@ search distance calls; the kernels count them and the tests check the count agai
 `e2e` is the same metric through pg_build_host with pinned host buffers: base + gt host->device
 and graph + projection device->host inside the timed region.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n N] [--d D]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--points N] [--dim D]
 
 --impl reference times the CPU restatement of the path (the oracle; the reference's own code for
 this path is GPU-only and its CPU RoarGraph path does not build on this Arm host) on all host
@@ -41,8 +41,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=1_000_000)
-    ap.add_argument("--d", type=int, default=200)
+    ap.add_argument("--points", dest="n", type=int, default=1_000_000)
+    ap.add_argument("--dim", dest="d", type=int, default=200)
     ap.add_argument("--degree", type=int, default=32)
     ap.add_argument("--beam", type=int, default=64)
     ap.add_argument("--seed", type=int, default=1234)
