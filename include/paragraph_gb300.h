@@ -182,6 +182,17 @@ int pg_prune_reverse_noalloc(void* stream, const float* d_base, uint64_t n, uint
                              uint32_t* d_pruned_num, uint32_t* d_reverse, uint32_t* d_reverse_num,
                              uint64_t* evals);
 
+/* Query-time search, search_shared_hashtable (Gsearcher.cuh:108-296): the same beam search over a
+ * built graph (n x graph_degree) for nq external query vectors (nq x d, e.g. the other modality),
+ * writing the best topk ids of each query's final list (out: nq x topk).  The reference never
+ * empties its shared visited set between the queries one warp handles, so its result depends on
+ * scheduling; here every query starts from an empty set. */
+int pg_query_search(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
+                    const uint32_t* d_graph, uint32_t graph_degree, const float* d_queries,
+                    uint64_t nq, uint32_t km, uint32_t kp, uint32_t kd, uint32_t reset_iter,
+                    uint32_t seed_base, uint32_t max_iters, uint32_t topk, uint32_t* d_out,
+                    uint64_t* evals, uint64_t* iters);
+
 /* ---- on-disk formats ----------------------------------------------------------------------- */
 /* Raw vectors as read by read_vec_from_file (include/utils.hpp:17-35): headerless, exactly
  * count*elem_size bytes, or with the Big-ANN [u32 n][u32 d] header (README.md:13-21) when

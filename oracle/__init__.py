@@ -55,6 +55,12 @@ def lib():
                                  ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
                                  ctypes.c_uint64, ctypes.c_uint64, _u32p, _u64p, _u32p]
         L.pgo_search.restype = ctypes.c_uint64
+        L.pgo_query_search.argtypes = [_f32p, ctypes.c_uint64, ctypes.c_uint32, _u32p,
+                                       ctypes.c_uint32, _f32p, ctypes.c_uint64, ctypes.c_uint32,
+                                       ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                       ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32, _u32p,
+                                       _u64p]
+        L.pgo_query_search.restype = ctypes.c_uint64
         L.pgo_dist_seq.argtypes = [_f32p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32]
         L.pgo_dist_seq.restype = ctypes.c_float
         L.pgo_dist_lane.argtypes = [_f32p, _f32p, ctypes.c_uint64]
@@ -157,6 +163,22 @@ def search(base, graph, km: int = 32, kp: int = 2, kd: int = 16, reset_iter: int
                           reset_iter, seed_base, max_iters, q_begin, q_end, _p(out, _u32p),
                           ctypes.byref(it), ctypes.byref(hit))
     return out, int(ev), int(it.value), bool(hit.value)
+
+
+def query_search(base, graph, queries, topk: int = 10, km: int = 32, kp: int = 2, kd: int = 16,
+                 reset_iter: int = 4, seed_base: int = 3030517, max_iters: int = 1 << 20):
+    """search_shared_hashtable (Gsearcher.cuh:108-296) with external queries: (ids nq x topk,
+    evals, iterations)."""
+    base = _f32(base)
+    graph = _u32(graph)
+    queries = _f32(queries)
+    n, d = base.shape
+    out = np.empty((queries.shape[0], topk), dtype=np.uint32)
+    it = ctypes.c_uint64(0)
+    ev = lib().pgo_query_search(_p(base, _f32p), n, d, _p(graph, _u32p), graph.shape[1],
+                                _p(queries, _f32p), queries.shape[0], km, kp, kd, reset_iter,
+                                seed_base, max_iters, topk, _p(out, _u32p), ctypes.byref(it))
+    return out, int(ev), int(it.value)
 
 
 class _Params(ctypes.Structure):

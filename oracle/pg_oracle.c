@@ -324,10 +324,9 @@ typedef struct {
  * out receives the km + kp*kd ids with the parent bit cleared. */
 static void search_one(const float* base, uint64_t n, uint64_t d, const uint32_t* graph,
                        uint32_t deg, uint32_t km, uint32_t kp, uint32_t kd, uint32_t reset_iter,
-                       uint32_t seed_base, uint64_t max_iters, uint32_t qid, vset* vs,
-                       float* dist, uint32_t* ids, uint32_t* out, search_stats* st) {
+                       uint32_t seed_base, uint64_t max_iters, const float* q, uint32_t out_width,
+                       vset* vs, float* dist, uint32_t* ids, uint32_t* out, search_stats* st) {
   const uint32_t L = km + kp * kd;
-  const float* q = base + (uint64_t)qid * d;
   for (uint32_t i = 0; i < kp * kd; i++) ids[km + i] = (uint32_t)((seed_base + (uint64_t)i) % n);
   for (uint32_t i = 0; i < km; i++) {
     dist[i] = FLT_MAX;
@@ -382,7 +381,7 @@ static void search_one(const float* base, uint64_t n, uint64_t d, const uint32_t
     }
   }
   st->iters += total_iters;
-  for (uint32_t i = 0; i < L; i++) out[i] = ids[i] & MASKED_TOMB;
+  for (uint32_t i = 0; i < L && i < out_width; i++) out[i] = ids[i] & MASKED_TOMB;
 }
 
 static uint32_t pow2_at_least(uint32_t x) {
@@ -412,7 +411,8 @@ uint64_t pgo_search(const float* base, uint64_t n, uint32_t d, const uint32_t* g
 #pragma omp for schedule(dynamic, 16)
     for (int64_t qi = (int64_t)q_begin; qi < (int64_t)q_end; qi++) {
       search_one(base, n, d, graph, deg, km, kp, kd, reset_iter, seed_base, max_iters,
-                 (uint32_t)qi, &vs, dist, ids, out + (uint64_t)(qi - (int64_t)q_begin) * L, &st);
+                 base + (uint64_t)qi * d, L, &vs, dist, ids,
+                 out + (uint64_t)(qi - (int64_t)q_begin) * L, &st);
     }
     ev_total += st.evals;
     it_total += st.iters;
@@ -423,6 +423,39 @@ uint64_t pgo_search(const float* base, uint64_t n, uint32_t d, const uint32_t* g
   }
   if (iters_out) *iters_out = it_total;
   if (cap_hit) *cap_hit = hit;
+  return ev_total;
+}
+
+/* search_shared_hashtable (Gsearcher.cuh:108-296): the same search for external query vectors,
+ * writing the first topk ids of each final list; the visited set starts empty for every query. */
+uint64_t pgo_query_search(const float* base, uint64_t n, uint32_t d, const uint32_t* graph,
+                          uint32_t deg, const float* queries, uint64_t nq, uint32_t km,
+                          uint32_t kp, uint32_t kd, uint32_t reset_iter, uint32_t seed_base,
+                          uint64_t max_iters, uint32_t topk, uint32_t* out, uint64_t* iters_out) {
+  const uint32_t L = km + kp * kd;
+  const uint32_t cap = pow2_at_least(2 * (km + (reset_iter + 1) * kp * kd) + 64);
+  uint64_t ev_total = 0, it_total = 0;
+#pragma omp parallel reduction(+ : ev_total, it_total)
+  {
+    vset vs;
+    vs.slot = (uint32_t*)malloc(sizeof(uint32_t) * cap);
+    vs.mask = cap - 1;
+    float* dist = (float*)malloc(sizeof(float) * L);
+    uint32_t* ids = (uint32_t*)malloc(sizeof(uint32_t) * L);
+    search_stats st = {0, 0, 0};
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t qi = 0; qi < (int64_t)nq; qi++) {
+      search_one(base, n, d, graph, deg, km, kp, kd, reset_iter, seed_base, max_iters,
+                 queries + (uint64_t)qi * d, topk, &vs, dist, ids, out + (uint64_t)qi * topk,
+                 &st);
+    }
+    ev_total += st.evals;
+    it_total += st.iters;
+    free(vs.slot);
+    free(dist);
+    free(ids);
+  }
+  if (iters_out) *iters_out = it_total;
   return ev_total;
 }
 

@@ -100,6 +100,8 @@ SIGNATURES = {
                                  _U32, _VP, _U64P, _U64P]),
     "pg_prune_reverse_noalloc": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _U32, _U32, _U32,
                                                 ctypes.c_int, _VP, _VP, _VP, _VP, _U64P]),
+    "pg_query_search": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _U32, _VP, _U64, _U32, _U32,
+                                       _U32, _U32, _U32, _U32, _U32, _VP, _U64P, _U64P]),
     "pg_read_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _VP, _U64, _U32P, _U32P]),
     "pg_save_graph": (ctypes.c_int, [ctypes.c_char_p, _VP, _U64, _U32, _U32]),
     "pg_entry_point": (ctypes.c_int, [_VP, _U64, _U32, _U64, _U32P]),
@@ -270,6 +272,19 @@ class Handle:
         _check(lib().pg_search(self._h, _ptr(base), n, d, _ptr(graph), graph.shape[1], km, kp, kd,
                                reset_iter, seed_base, max_iters, _ptr(out), ctypes.byref(ev),
                                ctypes.byref(it)))
+        return int(ev.value), int(it.value)
+
+
+    def query_search(self, base, graph, queries, out, km: int = 32, kp: int = 2, kd: int = 16,
+                     reset_iter: int = 4, seed_base: int = 3030517, max_iters: int = 1 << 20):
+        """search_shared_hashtable (Gsearcher.cuh:108-296): top out.shape[1] ids per query."""
+        n, d = base.shape
+        ev = ctypes.c_uint64(0)
+        it = ctypes.c_uint64(0)
+        _check(lib().pg_query_search(self._h, _ptr(base), n, d, _ptr(graph), graph.shape[1],
+                                     _ptr(queries), queries.shape[0], km, kp, kd, reset_iter,
+                                     seed_base, max_iters, out.shape[1], _ptr(out),
+                                     ctypes.byref(ev), ctypes.byref(it)))
         return int(ev.value), int(it.value)
 
 

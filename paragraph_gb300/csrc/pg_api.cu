@@ -361,6 +361,7 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
       sa.max_iters = p->max_search_iters;
       sa.order = nullptr;
       sa.out = sres;
+      sa.out_width = L;
       sa.evals = cnt + C_SEARCH + r;
       sa.iters = cnt + C_ITERS + r;
       sa.work = h->d_work + r;
@@ -841,6 +842,58 @@ int pg_search(pg_handle h, const float* d_base, uint64_t n, uint32_t d, const ui
   a.work = h->d_work;
   a.status = h->d_status;
   a.hash_slots = hash_slots_for(km, reset_iter, kp * kd);
+  a.out_width = km + kp * kd;
+  PG_CUDA(pg::launch_search(a, h->num_sms, h->smem_optin, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_counters, h->d_counters, 16, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  if (evals) *evals = h->h_counters[0];
+  if (iters) *iters = h->h_counters[1];
+  return status_to_error(*h->h_status);
+}
+
+int pg_query_search(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
+                    const uint32_t* d_graph, uint32_t graph_degree, const float* d_queries,
+                    uint64_t nq, uint32_t km, uint32_t kp, uint32_t kd, uint32_t reset_iter,
+                    uint32_t seed_base, uint32_t max_iters, uint32_t topk, uint32_t* d_out,
+                    uint64_t* evals, uint64_t* iters) {
+  if (!h || !d_base || !d_graph || !d_queries || !d_out) return fail(PG_EINVAL, "NULL argument");
+  if (n == 0 || n >= 0x7FFFFFFFull || nq == 0 || nq >= 0x7FFFFFFFull)
+    return fail(PG_EINVAL, "bad n or nq");
+  if (!pg::search_supported(d, km, kp, kd))
+    return fail(PG_EUNSUPPORTED, "search supports kp*kd == 32, km in {32,64,96}, d <= 512, d %% 4 == 0");
+  if (kd > graph_degree) return fail(PG_EINVAL, "kd exceeds graph_degree");
+  if (reset_iter < 1) return fail(PG_EINVAL, "reset_iter must be positive");
+  if (topk < 1 || topk > km + kp * kd) return fail(PG_EINVAL, "topk must be in [1, km + kp*kd]");
+  if (!aligned16(d_base) || !aligned16(d_queries))
+    return fail(PG_EINVAL, "base and queries must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  cudaStream_t s = h->stream;
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, s));
+  PG_CUDA(cudaMemsetAsync(h->d_counters, 0, 16, s));
+  PG_CUDA(cudaMemsetAsync(h->d_work, 0, 4, s));
+  pg::SearchArgs a{};
+  a.base = d_base;
+  a.n = n;
+  a.d = d;
+  a.graph = d_graph;
+  a.graph_degree = graph_degree;
+  a.km = km;
+  a.kp = kp;
+  a.kd = kd;
+  a.reset_iter = reset_iter;
+  a.seed_base = seed_base;
+  a.max_iters = max_iters;
+  a.out = d_out;
+  a.evals = h->d_counters;
+  a.iters = h->d_counters + 1;
+  a.work = h->d_work;
+  a.status = h->d_status;
+  a.hash_slots = hash_slots_for(km, reset_iter, kp * kd);
+  a.queries = d_queries;
+  a.nq = nq;
+  a.out_width = topk;
   PG_CUDA(pg::launch_search(a, h->num_sms, h->smem_optin, s));
   PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, s));
   PG_CUDA(cudaMemcpyAsync(h->h_counters, h->d_counters, 16, cudaMemcpyDeviceToHost, s));

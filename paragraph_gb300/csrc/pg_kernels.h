@@ -64,6 +64,11 @@ struct SearchArgs {
   uint32_t hash_slots;    // visited-set capacity per warp (power of two)
   const uint64_t* seg_off;  // batched builds: sub-index node offsets (seg_count + 1), else NULL
   uint32_t seg_count;
+  // query search (search_shared_hashtable): nq external query vectors (nq x d) instead of the
+  // base points; NULL for the build's link rounds
+  const float* queries;
+  uint64_t nq;
+  uint32_t out_width;  // ids written per query: L for link rounds, top-k for a query search
 };
 
 cudaError_t launch_match_winner(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint64_t n,

@@ -225,9 +225,9 @@ __global__ void __launch_bounds__(32) k_search(SearchArgs a) {
     uint32_t qi = 0;
     if (lane == 0) qi = atomicAdd(a.work, 1u);
     qi = __shfl_sync(kFull, qi, 0);
-    if (qi >= a.n) break;
+    if (qi >= (a.queries ? a.nq : a.n)) break;
     const uint32_t qid = a.order ? a.order[qi] : qi;
-    const float* qrow = a.base + static_cast<uint64_t>(qid) * a.d;
+    const float* qrow = (a.queries ? a.queries : a.base) + static_cast<uint64_t>(qid) * a.d;
     Q4<KSTEPS> q;
 #pragma unroll
     for (int k = 0; k < KSTEPS; k++) {
@@ -342,11 +342,11 @@ __global__ void __launch_bounds__(32) k_search(SearchArgs a) {
     }
     if (!ok) break;
     it_all += (lane == 0) ? total : 0u;
-    uint32_t* orow = a.out + static_cast<uint64_t>(qid) * L;
+    uint32_t* orow = a.out + static_cast<uint64_t>(qid) * a.out_width;
 #pragma unroll
     for (int s = 0; s < E; s++) {
       const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
-      if (i < L) orow[i] = id[s] & kMaskedTomb;
+      if (i < L && i < a.out_width) orow[i] = id[s] & kMaskedTomb;
     }
   }
   if (!ok) {
@@ -501,7 +501,6 @@ __global__ void __launch_bounds__(32, KSTEPS <= 8 ? 20 : 12) k_search_m32(Search
   float* rows = reinterpret_cast<float*>(smem_raw + 16 + 256 + 128 + 4u * a.hash_slots);
   const uint32_t hmask = a.hash_slots - 1u;
   const uint32_t kp = a.kp, kd = a.kd;
-  constexpr uint32_t L = 64;
   if (lane == 0) mbar_init(mbar, 1);
   __syncwarp();
   uint32_t phase = 0;
@@ -514,9 +513,9 @@ __global__ void __launch_bounds__(32, KSTEPS <= 8 ? 20 : 12) k_search_m32(Search
     uint32_t qi = 0;
     if (lane == 0) qi = atomicAdd(a.work, 1u);
     qi = __shfl_sync(kFull, qi, 0);
-    if (qi >= a.n) break;
+    if (qi >= (a.queries ? a.nq : a.n)) break;
     const uint32_t qid = a.order ? a.order[qi] : qi;
-    const float* qrow = a.base + static_cast<uint64_t>(qid) * a.d;
+    const float* qrow = (a.queries ? a.queries : a.base) + static_cast<uint64_t>(qid) * a.d;
     Q4<KSTEPS> q;
 #pragma unroll
     for (int k = 0; k < KSTEPS; k++) {
@@ -648,9 +647,9 @@ __global__ void __launch_bounds__(32, KSTEPS <= 8 ? 20 : 12) k_search_m32(Search
     uint64_t k2[2] = {top_key, cand_key};
     uint32_t i2[2] = {top_id, cand_id};
     warp_sort_kv<2>(k2, i2);
-    uint32_t* orow = a.out + static_cast<uint64_t>(qid) * L;
-    orow[lane] = i2[0] & kMaskedTomb;
-    orow[32 + lane] = i2[1] & kMaskedTomb;
+    uint32_t* orow = a.out + static_cast<uint64_t>(qid) * a.out_width;
+    if (lane < a.out_width) orow[lane] = i2[0] & kMaskedTomb;
+    if (32 + lane < a.out_width) orow[32 + lane] = i2[1] & kMaskedTomb;
   }
   if (!ok) {
     if (lane == 0) raise_error(a.status, kErrWait);
@@ -683,7 +682,8 @@ static cudaError_t launch_search_m32(const SearchArgs& a, int num_sms, size_t sm
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   uint64_t blocks = static_cast<uint64_t>(num_sms) * per_sm;
-  if (blocks > a.n) blocks = a.n;
+  const uint64_t nq = a.queries ? a.nq : a.n;
+  if (blocks > nq) blocks = nq;
   kern<<<static_cast<unsigned>(blocks), 32, smem, st>>>(a);
   return cudaGetLastError();
 }
@@ -711,7 +711,8 @@ static cudaError_t launch_search_t(const SearchArgs& a, int num_sms, size_t smem
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   uint64_t blocks = static_cast<uint64_t>(num_sms) * per_sm;
-  if (blocks > a.n) blocks = a.n;
+  const uint64_t nq = a.queries ? a.nq : a.n;
+  if (blocks > nq) blocks = nq;
   k_search<KM_S, KS><<<static_cast<unsigned>(blocks), 32, smem, st>>>(a);
   return cudaGetLastError();
 }
