@@ -96,6 +96,20 @@ typedef struct pg_stats {
 
 typedef struct pg_handle_s* pg_handle;
 
+/* Launch-shape choices of a handle.  None of them changes a result: every choice builds the same
+ * graph bit for bit; they only move time.  Zero fields mean the library's defaults. */
+typedef struct pg_tuning {
+  uint32_t search_rows;         /* candidate rows staged per pass in the Km=32 search: 8 or 16 */
+  uint32_t search_warps_per_sm; /* cap on resident search warps per SM (0 = occupancy maximum) */
+  uint32_t hash_factor;         /* visited-set capacity multiplier over the exact minimum: 1, 2, 4 */
+  uint32_t screen_carveout;     /* shared-memory carveout (%) of the screened prune (0 = 76) */
+  uint32_t beam;                /* L chosen by pg_autotune's recall target (0 = not tuned) */
+  float recall;                 /* recall@10 measured for `beam` (when tuned) */
+  float ms_build;               /* build time measured with this tuning */
+  float ms_default;             /* build time measured with the defaults */
+  uint32_t reserved[8];
+} pg_tuning;
+
 /* ---- library ---------------------------------------------------------------------------- */
 const char* pg_last_error(void);
 uint32_t pg_abi_version(void);
@@ -130,6 +144,24 @@ int pg_build_batched_device(pg_handle h, const pg_params* p, const float* d_base
                             const uint32_t* d_gt, const uint64_t* node_off,
                             const uint64_t* query_off, uint32_t count, uint32_t* d_graph,
                             uint32_t* d_proj, pg_stats* st);
+
+/* ---- autotuning (no counterpart in the reference: its launch shapes, beam width and hash
+ * capacity are compile-time constants, tests/test_t2iend.cu:671-727) --------------------------
+ * pg_set_tuning / pg_get_tuning: the tuning later builds on this handle use.
+ * pg_autotune: times trial builds of the given data and keeps the fastest choice of search
+ * staging rows, resident search warps, visited-set capacity and screened-prune carveout
+ * (coordinate search from the defaults, each candidate timed twice, kept only when it wins by
+ * more than 1%).  When d_queries (the training queries behind d_gt, q_i x d per sub-index) and
+ * target_recall > 0 are given, it first picks the beam: the smallest L in {64, 96, 128} whose
+ * graph reaches target_recall recall@10 (pg_query_search of up to 1000 training queries of the
+ * largest sub-index against their exact top-10 in d_gt), else the L with the best recall; p->km
+ * is updated.  The tuning is stored in the handle and returned in *out.  A single index is
+ * count = 1, node_off = {0, n}, query_off = {0, q}. */
+int pg_set_tuning(pg_handle h, const pg_tuning* t);
+int pg_get_tuning(pg_handle h, pg_tuning* t);
+int pg_autotune(pg_handle h, pg_params* p, const float* d_base, uint32_t d, const uint32_t* d_gt,
+                const uint64_t* node_off, const uint64_t* query_off, uint32_t count,
+                const float* d_queries, float target_recall, pg_tuning* out);
 
 /* ---- stages: one entry point per reference kernel, device pointers, handle's stream ------ */
 /* K0 match_top1_kernel_v0 (Gbuilder.cuh:104-135, launched tests/test_t2iend.cu:976): for each

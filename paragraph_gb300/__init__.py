@@ -70,6 +70,18 @@ class Stats(ctypes.Structure):
         return out
 
 
+class Tuning(ctypes.Structure):
+    """pg_tuning: launch shapes of a handle (results do not depend on them)."""
+    _fields_ = [("search_rows", ctypes.c_uint32), ("search_warps_per_sm", ctypes.c_uint32),
+                ("hash_factor", ctypes.c_uint32), ("screen_carveout", ctypes.c_uint32),
+                ("beam", ctypes.c_uint32), ("recall", ctypes.c_float),
+                ("ms_build", ctypes.c_float), ("ms_default", ctypes.c_float),
+                ("reserved", ctypes.c_uint32 * 8)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 _LIB = None
 _VP = ctypes.c_void_p
 _U64 = ctypes.c_uint64
@@ -102,6 +114,10 @@ SIGNATURES = {
                                                 ctypes.c_int, _VP, _VP, _VP, _VP, _U64P]),
     "pg_query_search": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _U32, _VP, _U64, _U32, _U32,
                                        _U32, _U32, _U32, _U32, _U32, _VP, _U64P, _U64P]),
+    "pg_set_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
+    "pg_get_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
+    "pg_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _U32, _VP, _VP, _VP, _U32,
+                                   _VP, ctypes.c_float, ctypes.POINTER(Tuning)]),
     "pg_read_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _VP, _U64, _U32P, _U32P]),
     "pg_save_graph": (ctypes.c_int, [ctypes.c_char_p, _VP, _U64, _U32, _U32]),
     "pg_entry_point": (ctypes.c_int, [_VP, _U64, _U32, _U64, _U32P]),
@@ -274,6 +290,30 @@ class Handle:
                                ctypes.byref(it)))
         return int(ev.value), int(it.value)
 
+
+    def set_tuning(self, tuning: Tuning):
+        _check(lib().pg_set_tuning(self._h, ctypes.byref(tuning)))
+
+    def get_tuning(self) -> Tuning:
+        t = Tuning()
+        _check(lib().pg_get_tuning(self._h, ctypes.byref(t)))
+        return t
+
+    def autotune(self, base, gt, params: Params | None = None, node_off=None, query_off=None,
+                 queries=None, target_recall: float = 0.0) -> tuple[Params, Tuning]:
+        """pg_autotune over device tensors (one index, or a batched table).  Returns the params
+        (km updated when a recall target picked the beam) and the tuning now set on the handle."""
+        params = params or default_params()
+        p = Params.from_buffer_copy(params)
+        if node_off is None:
+            node_off, query_off = [0, base.shape[0]], [0, gt.shape[0]]
+        no = np.ascontiguousarray(node_off, dtype=np.uint64)
+        qo = np.ascontiguousarray(query_off, dtype=np.uint64)
+        t = Tuning()
+        _check(lib().pg_autotune(self._h, ctypes.byref(p), _ptr(base), base.shape[1], _ptr(gt),
+                                 no.ctypes.data, qo.ctypes.data, len(no) - 1, _ptr(queries),
+                                 float(target_recall), ctypes.byref(t)))
+        return p, t
 
     def query_search(self, base, graph, queries, out, km: int = 32, kp: int = 2, kd: int = 16,
                      reset_iter: int = 4, seed_base: int = 3030517, max_iters: int = 1 << 20):

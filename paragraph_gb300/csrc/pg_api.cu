@@ -136,6 +136,7 @@ struct pg_handle_s {
   size_t segs_cap = 0;
   cudaGraphExec_t gexec = nullptr;  // captured build (PG_FLAG_CUDA_GRAPH) and what it was built for
   GraphKey gkey;
+  pg_tuning tune{};  // launch shapes of later builds (zero = defaults)
   std::mutex mu;
 };
 
@@ -345,7 +346,8 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
 
     const uint32_t* g = proj;
     uint32_t gdeg = p->proj_degree;
-    const uint32_t hslots = hash_slots_for(p->km, p->reset_iter, p->kp * p->kd);
+    const uint32_t hslots = hash_slots_for(p->km, p->reset_iter, p->kp * p->kd) *
+                            std::max(1u, h->tune.hash_factor);
     for (uint32_t r = 0; r < p->link_rounds; r++) {
       pg::SearchArgs sa{};
       sa.base = base;
@@ -369,6 +371,8 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
       sa.hash_slots = hslots;
       sa.seg_off = d_seg;
       sa.seg_count = seg_count;
+      sa.rows = h->tune.search_rows;
+      sa.max_blocks_per_sm = h->tune.search_warps_per_sm;
       PG_CUDA(pg::launch_search(sa, sms, h->smem_optin, s));
       if (stage_events) PG_CUDA(cudaEventRecord(h->ev[2 + 3 * r], s));
       PG_CUDA(cudaMemsetAsync(indeg, 0, n * 4, s));
@@ -387,6 +391,7 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
       pr.evals = cnt + C_PRUNE + r;
       pr.status = h->d_status;
       pr.rescored = cnt + C_RESCORED + r;
+      pr.carveout = h->tune.screen_carveout;
       if (p->screen == PG_SCREEN_BF16 && pg::screen_supported(pr.c, d, pr.strict))
         PG_CUDA(pg::launch_prune_screen(pr, sms, h->smem_optin, s));
       else
@@ -502,6 +507,58 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
     }
   }
   return PG_OK;
+}
+
+// pg_query_search without taking the handle's lock (callers hold it).
+int query_search_locked(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
+                        const uint32_t* d_graph, uint32_t graph_degree, const float* d_queries,
+                        uint64_t nq, uint32_t km, uint32_t kp, uint32_t kd, uint32_t reset_iter,
+                        uint32_t seed_base, uint32_t max_iters, uint32_t topk, uint32_t* d_out,
+                        uint64_t* evals, uint64_t* iters) {
+  if (n == 0 || n >= 0x7FFFFFFFull || nq == 0 || nq >= 0x7FFFFFFFull)
+    return fail(PG_EINVAL, "bad n or nq");
+  if (!pg::search_supported(d, km, kp, kd))
+    return fail(PG_EUNSUPPORTED, "search supports kp*kd == 32, km in {32,64,96}, d <= 512, d %% 4 == 0");
+  if (kd > graph_degree) return fail(PG_EINVAL, "kd exceeds graph_degree");
+  if (reset_iter < 1) return fail(PG_EINVAL, "reset_iter must be positive");
+  if (topk < 1 || topk > km + kp * kd) return fail(PG_EINVAL, "topk must be in [1, km + kp*kd]");
+  if (!aligned16(d_base) || !aligned16(d_queries))
+    return fail(PG_EINVAL, "base and queries must be 16-byte aligned");
+  PG_CUDA(cudaSetDevice(h->device));
+  cudaStream_t s = h->stream;
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, s));
+  PG_CUDA(cudaMemsetAsync(h->d_counters, 0, 16, s));
+  PG_CUDA(cudaMemsetAsync(h->d_work, 0, 4, s));
+  pg::SearchArgs a{};
+  a.base = d_base;
+  a.n = n;
+  a.d = d;
+  a.graph = d_graph;
+  a.graph_degree = graph_degree;
+  a.km = km;
+  a.kp = kp;
+  a.kd = kd;
+  a.reset_iter = reset_iter;
+  a.seed_base = seed_base;
+  a.max_iters = max_iters;
+  a.out = d_out;
+  a.evals = h->d_counters;
+  a.iters = h->d_counters + 1;
+  a.work = h->d_work;
+  a.status = h->d_status;
+  a.hash_slots = hash_slots_for(km, reset_iter, kp * kd);
+  a.queries = d_queries;
+  a.nq = nq;
+  a.out_width = topk;
+  a.rows = h->tune.search_rows;
+  a.max_blocks_per_sm = h->tune.search_warps_per_sm;
+  PG_CUDA(pg::launch_search(a, h->num_sms, h->smem_optin, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaMemcpyAsync(h->h_counters, h->d_counters, 16, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  if (evals) *evals = h->h_counters[0];
+  if (iters) *iters = h->h_counters[1];
+  return status_to_error(*h->h_status);
 }
 
 }  // namespace
@@ -858,49 +915,214 @@ int pg_query_search(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
                     uint32_t seed_base, uint32_t max_iters, uint32_t topk, uint32_t* d_out,
                     uint64_t* evals, uint64_t* iters) {
   if (!h || !d_base || !d_graph || !d_queries || !d_out) return fail(PG_EINVAL, "NULL argument");
-  if (n == 0 || n >= 0x7FFFFFFFull || nq == 0 || nq >= 0x7FFFFFFFull)
-    return fail(PG_EINVAL, "bad n or nq");
-  if (!pg::search_supported(d, km, kp, kd))
-    return fail(PG_EUNSUPPORTED, "search supports kp*kd == 32, km in {32,64,96}, d <= 512, d %% 4 == 0");
-  if (kd > graph_degree) return fail(PG_EINVAL, "kd exceeds graph_degree");
-  if (reset_iter < 1) return fail(PG_EINVAL, "reset_iter must be positive");
-  if (topk < 1 || topk > km + kp * kd) return fail(PG_EINVAL, "topk must be in [1, km + kp*kd]");
-  if (!aligned16(d_base) || !aligned16(d_queries))
+  std::lock_guard<std::mutex> lk(h->mu);
+  return query_search_locked(h, d_base, n, d, d_graph, graph_degree, d_queries, nq, km, kp, kd,
+                             reset_iter, seed_base, max_iters, topk, d_out, evals, iters);
+}
+
+// ---------------------------------------------------------------- autotuning
+
+int pg_set_tuning(pg_handle h, const pg_tuning* t) {
+  if (!h || !t) return fail(PG_EINVAL, "NULL argument");
+  if (t->search_rows != 0 && t->search_rows != 8 && t->search_rows != 16)
+    return fail(PG_EINVAL, "search_rows=%u must be 0, 8 or 16", t->search_rows);
+  if (t->search_warps_per_sm > 64) return fail(PG_EINVAL, "search_warps_per_sm must be <= 64");
+  if (t->hash_factor > 4 || t->hash_factor == 3)
+    return fail(PG_EINVAL, "hash_factor=%u must be 0, 1, 2 or 4", t->hash_factor);
+  if (t->screen_carveout > 100) return fail(PG_EINVAL, "screen_carveout must be <= 100");
+  std::lock_guard<std::mutex> lk(h->mu);
+  h->tune = *t;
+  if (h->gexec) {  // a captured build holds the old launch shapes
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  return PG_OK;
+}
+
+int pg_get_tuning(pg_handle h, pg_tuning* t) {
+  if (!h || !t) return fail(PG_EINVAL, "NULL argument");
+  std::lock_guard<std::mutex> lk(h->mu);
+  *t = h->tune;
+  return PG_OK;
+}
+
+int pg_autotune(pg_handle h, pg_params* p, const float* d_base, uint32_t d, const uint32_t* d_gt,
+                const uint64_t* node_off, const uint64_t* query_off, uint32_t count,
+                const float* d_queries, float target_recall, pg_tuning* out) {
+  if (!h || !p) return fail(PG_EINVAL, "NULL argument");
+  if (!node_off || !query_off || count == 0) return fail(PG_EINVAL, "empty sub-index table");
+  if (node_off[0] != 0 || query_off[0] != 0) return fail(PG_EINVAL, "offsets must start at 0");
+  for (uint32_t i = 0; i < count; i++) {
+    if (node_off[i + 1] <= node_off[i]) return fail(PG_EINVAL, "sub-index %u is empty", i);
+    if (query_off[i + 1] < query_off[i]) return fail(PG_EINVAL, "query offsets must ascend");
+  }
+  const uint64_t n = node_off[count], q = query_off[count];
+  int rc = check_params(p, n, d, q);
+  if (rc) return rc;
+  if (!d_base || !d_gt) return fail(PG_EINVAL, "base and gt must be device pointers");
+  if (!aligned16(d_base) || (d_queries && !aligned16(d_queries)))
     return fail(PG_EINVAL, "base and queries must be 16-byte aligned");
   std::lock_guard<std::mutex> lk(h->mu);
   PG_CUDA(cudaSetDevice(h->device));
-  cudaStream_t s = h->stream;
-  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, s));
-  PG_CUDA(cudaMemsetAsync(h->d_counters, 0, 16, s));
-  PG_CUDA(cudaMemsetAsync(h->d_work, 0, 4, s));
-  pg::SearchArgs a{};
-  a.base = d_base;
-  a.n = n;
-  a.d = d;
-  a.graph = d_graph;
-  a.graph_degree = graph_degree;
-  a.km = km;
-  a.kp = kp;
-  a.kd = kd;
-  a.reset_iter = reset_iter;
-  a.seed_base = seed_base;
-  a.max_iters = max_iters;
-  a.out = d_out;
-  a.evals = h->d_counters;
-  a.iters = h->d_counters + 1;
-  a.work = h->d_work;
-  a.status = h->d_status;
-  a.hash_slots = hash_slots_for(km, reset_iter, kp * kd);
-  a.queries = d_queries;
-  a.nq = nq;
-  a.out_width = topk;
-  PG_CUDA(pg::launch_search(a, h->num_sms, h->smem_optin, s));
-  PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, s));
-  PG_CUDA(cudaMemcpyAsync(h->h_counters, h->d_counters, 16, cudaMemcpyDeviceToHost, s));
-  PG_CUDA(cudaStreamSynchronize(s));
-  if (evals) *evals = h->h_counters[0];
-  if (iters) *iters = h->h_counters[1];
-  return status_to_error(*h->h_status);
+  pg_params tp = *p;
+  tp.flags &= ~PG_FLAG_CUDA_GRAPH;  // per-stage timing
+  uint32_t* g = nullptr;
+  uint32_t* pj = nullptr;
+  uint32_t* qout = nullptr;
+  const pg_tuning saved = h->tune;
+  struct Cleanup {
+    uint32_t** bufs[3];
+    ~Cleanup() {
+      for (auto b : bufs)
+        if (*b) cudaFree(*b);
+    }
+  } cleanup{{&g, &pj, &qout}};
+  PG_CUDA(cudaMalloc(&g, n * tp.degree * 4));
+  PG_CUDA(cudaMalloc(&pj, n * tp.proj_degree * 4));
+  auto build = [&](const pg_params& bp, pg_stats* st) -> int {
+    std::memset(st, 0, sizeof(*st));
+    if (count > 1)
+      return run_build(h, &bp, d_base, n, d, d_gt, q, g, pj, st, node_off, query_off, count);
+    return run_build(h, &bp, d_base, n, d, d_gt, q, g, pj, st);
+  };
+  auto restore = [&](int code) {
+    h->tune = saved;
+    return code;
+  };
+  pg_tuning best{};
+  best.search_rows = 8;
+  best.hash_factor = 1;
+  best.screen_carveout = 76;
+  h->tune = best;
+  pg_stats st;
+
+  // 1) beam: the smallest L reaching the recall target on training queries of the largest
+  //    sub-index (their exact top-10 is the first ten ground-truth ids)
+  if (d_queries && target_recall > 0.0f && tp.kp * tp.kd == 32 && tp.link_rounds > 0) {
+    uint32_t big = 0;
+    for (uint32_t i = 1; i < count; i++)
+      if (node_off[i + 1] - node_off[i] > node_off[big + 1] - node_off[big]) big = i;
+    const uint64_t ni = node_off[big + 1] - node_off[big];
+    const uint64_t ns = std::min<uint64_t>(query_off[big + 1] - query_off[big], 1000);
+    if (ns > 0) {
+      constexpr uint32_t kTop = 10;
+      std::vector<uint32_t> truth(ns * tp.gt_k), got(ns * kTop);
+      PG_CUDA(cudaMemcpy(truth.data(), d_gt + query_off[big] * tp.gt_k, truth.size() * 4,
+                         cudaMemcpyDeviceToHost));
+      PG_CUDA(cudaMalloc(&qout, ns * kTop * 4));
+      float best_rec = -1.0f, chosen_rec = -1.0f;
+      uint32_t best_beam = 0, chosen = 0;
+      for (uint32_t beam : {64u, 96u, 128u}) {
+        pg_params bp = tp;
+        bp.km = beam - bp.kp * bp.kd;
+        if (check_params(&bp, n, d, q) != PG_OK) continue;
+        rc = build(bp, &st);
+        if (rc) return restore(rc);
+        rc = query_search_locked(h, d_base + node_off[big] * d, ni, d,
+                                 g + node_off[big] * bp.degree, bp.degree,
+                                 d_queries + query_off[big] * d, ns, bp.km, bp.kp, bp.kd,
+                                 bp.reset_iter, bp.seed_base, bp.max_search_iters, kTop, qout,
+                                 nullptr, nullptr);
+        if (rc) return restore(rc);
+        PG_CUDA(cudaMemcpy(got.data(), qout, got.size() * 4, cudaMemcpyDeviceToHost));
+        double hit = 0, tot = 0;
+        for (uint64_t i = 0; i < ns; i++) {
+          const uint32_t* tr = truth.data() + i * tp.gt_k;
+          const uint32_t* gg = got.data() + i * kTop;
+          for (uint32_t a = 0; a < kTop; a++) {
+            if (tr[a] == PG_TOMB) continue;
+            tot += 1;
+            for (uint32_t b = 0; b < kTop; b++)
+              if (gg[b] == tr[a]) {
+                hit += 1;
+                break;
+              }
+          }
+        }
+        const float rec = tot > 0 ? static_cast<float>(hit / tot) : 0.0f;
+        if (rec > best_rec) {
+          best_rec = rec;
+          best_beam = beam;
+        }
+        if (rec >= target_recall) {
+          chosen = beam;
+          chosen_rec = rec;
+          break;
+        }
+      }
+      if (!chosen) {
+        chosen = best_beam;
+        chosen_rec = best_rec;
+      }
+      if (chosen) {
+        tp.km = chosen - tp.kp * tp.kd;
+        best.beam = chosen;
+        best.recall = chosen_rec;
+      }
+    }
+  }
+
+  // 2) launch shapes: coordinate search from the defaults, best of two builds per candidate
+  auto measure = [&](const pg_tuning& t, float* ms) -> int {
+    h->tune = t;
+    float m = 1e30f;
+    for (int rep = 0; rep < 2; rep++) {
+      const int r = build(tp, &st);
+      if (r) return r;
+      m = std::min(m, st.ms_total);
+    }
+    *ms = m;
+    return PG_OK;
+  };
+  rc = build(tp, &st);  // warm-up (workspace, first launches)
+  if (rc) return restore(rc);
+  float cur = 0.0f;
+  rc = measure(best, &cur);
+  if (rc) return restore(rc);
+  best.ms_default = cur;
+  auto try_value = [&](uint32_t pg_tuning::*field, uint32_t value) -> int {
+    pg_tuning t = best;
+    t.*field = value;
+    float ms = 0.0f;
+    const int r = measure(t, &ms);
+    if (r == PG_ECUDA && g_err.find("invalid argument") != std::string::npos)
+      return PG_OK;  // a shape this device cannot launch (e.g. shared memory): skip it
+    if (r) return r;
+    if (ms < cur * 0.99f) {
+      best = t;
+      cur = ms;
+    }
+    return PG_OK;
+  };
+  if (tp.link_rounds > 0) {
+    if (tp.km == 32) {
+      rc = try_value(&pg_tuning::search_rows, 16);
+      if (rc) return restore(rc);
+    }
+    for (uint32_t w : {16u, 12u, 8u}) {
+      rc = try_value(&pg_tuning::search_warps_per_sm, w);
+      if (rc) return restore(rc);
+    }
+    for (uint32_t f : {2u, 4u}) {
+      rc = try_value(&pg_tuning::hash_factor, f);
+      if (rc) return restore(rc);
+    }
+    if (tp.screen == PG_SCREEN_BF16) {
+      for (uint32_t c : {50u, 100u, 25u}) {
+        rc = try_value(&pg_tuning::screen_carveout, c);
+        if (rc) return restore(rc);
+      }
+    }
+  }
+  best.ms_build = cur;
+  h->tune = best;
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  p->km = tp.km;
+  if (out) *out = best;
+  return PG_OK;
 }
 
 // ---------------------------------------------------------------- file formats

@@ -28,6 +28,9 @@ struct PruneArgs {
   const uint64_t* seg_off;
   const uint64_t* qseg_off;
   uint32_t seg_count;
+  // screened kernel: preferred shared-memory carveout in percent (0 = 76); results do not
+  // depend on it
+  uint32_t carveout;
 };
 
 struct MergeArgs {
@@ -69,6 +72,10 @@ struct SearchArgs {
   const float* queries;
   uint64_t nq;
   uint32_t out_width;  // ids written per query: L for link rounds, top-k for a query search
+  // launch shape (results do not depend on it): candidate rows staged per pass (8 or 16, Km = 32
+  // kernel) and a cap on resident search warps per SM; 0 = defaults
+  uint32_t rows;
+  uint32_t max_blocks_per_sm;
 };
 
 cudaError_t launch_match_winner(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint64_t n,

@@ -345,8 +345,8 @@ __global__ void __launch_bounds__(32, 16) k_prune_screen(PruneArgs a) {
 
 template <typename Args>
 static cudaError_t launch_screen_kernel(void (*kern)(Args), const Args& a, uint64_t n,
-                                        uint32_t d, int num_sms, size_t smem_optin,
-                                        cudaStream_t st) {
+                                        uint32_t d, uint32_t carveout, int num_sms,
+                                        size_t smem_optin, cudaStream_t st) {
   const size_t smem = screen_smem_per_warp(d);
   if (smem > smem_optin) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -356,8 +356,10 @@ static cudaError_t launch_screen_kernel(void (*kern)(Args), const Args& a, uint6
   // warps: keep about a quarter of the unified L1/shared capacity as L1 (measured on GB300 at
   // 1M x 200: 22 ms per prune round with this split against 35 ms with the largest shared
   // carveout).  A screened merge (K7/K11) built the same way was slower than the plain merge at
-  // every list-length split tried: most merged lists hold 32 entries or fewer.
-  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 76);
+  // every list-length split tried: most merged lists hold 32 entries or fewer.  The autotuner
+  // may pick another split (`carveout`).
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           carveout ? static_cast<int>(carveout) : 76);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem);
@@ -372,7 +374,8 @@ static cudaError_t launch_screen_kernel(void (*kern)(Args), const Args& a, uint6
 cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_optin,
                                 cudaStream_t st) {
   if (!screen_supported(a.c, a.d, a.strict)) return cudaErrorInvalidValue;
-  return launch_screen_kernel(k_prune_screen, a, a.n, a.d, num_sms, smem_optin, st);
+  if (a.carveout > 100) return cudaErrorInvalidValue;
+  return launch_screen_kernel(k_prune_screen, a, a.n, a.d, a.carveout, num_sms, smem_optin, st);
 }
 
 }  // namespace pg

@@ -661,25 +661,24 @@ __global__ void __launch_bounds__(32, KSTEPS <= 8 ? 20 : 12) k_search_m32(Search
   }
 }
 
-constexpr int kM32Rows = 8;
-
-size_t search_m32_smem(uint32_t d, uint32_t hash_slots) {
-  return 16 + 256 + 128 + 4 * static_cast<size_t>(hash_slots) +
-         static_cast<size_t>(kM32Rows) * 4 * d;
+size_t search_m32_smem(uint32_t d, uint32_t hash_slots, uint32_t rows) {
+  return 16 + 256 + 128 + 4 * static_cast<size_t>(hash_slots) + static_cast<size_t>(rows) * 4 * d;
 }
 
-template <int KS>
+template <int KS, int ROWS>
 static cudaError_t launch_search_m32(const SearchArgs& a, int num_sms, size_t smem_optin,
                                      cudaStream_t st) {
-  const size_t smem = search_m32_smem(a.d, a.hash_slots);
+  const size_t smem = search_m32_smem(a.d, a.hash_slots, ROWS);
   if (smem > smem_optin) return cudaErrorInvalidValue;
-  auto kern = k_search_m32<KS, kM32Rows>;
+  auto kern = k_search_m32<KS, ROWS>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem);
   if (e != cudaSuccess) return e;
+  if (a.max_blocks_per_sm && per_sm > static_cast<int>(a.max_blocks_per_sm))
+    per_sm = static_cast<int>(a.max_blocks_per_sm);
   if (per_sm < 1) per_sm = 1;
   uint64_t blocks = static_cast<uint64_t>(num_sms) * per_sm;
   const uint64_t nq = a.queries ? a.nq : a.n;
@@ -709,6 +708,8 @@ static cudaError_t launch_search_t(const SearchArgs& a, int num_sms, size_t smem
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<KM_S, KS>, 32, smem);
   if (e != cudaSuccess) return e;
+  if (a.max_blocks_per_sm && per_sm > static_cast<int>(a.max_blocks_per_sm))
+    per_sm = static_cast<int>(a.max_blocks_per_sm);
   if (per_sm < 1) per_sm = 1;
   uint64_t blocks = static_cast<uint64_t>(num_sms) * per_sm;
   const uint64_t nq = a.queries ? a.nq : a.n;
@@ -721,11 +722,18 @@ cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, c
   if (!search_supported(a.d, a.km, a.kp, a.kd)) return cudaErrorInvalidValue;
   const int km_s = static_cast<int>(a.km / 32);
   const bool small = a.d <= 256;
+  if (a.rows != 0 && a.rows != 8 && a.rows != 16) return cudaErrorInvalidValue;
+  const bool r16 = a.rows == 16;
   switch (km_s) {
     case 1:
-      if (a.d <= 224) return launch_search_m32<7>(a, num_sms, smem_optin, st);
-      return small ? launch_search_m32<8>(a, num_sms, smem_optin, st)
-                   : launch_search_m32<16>(a, num_sms, smem_optin, st);
+      if (a.d <= 224)
+        return r16 ? launch_search_m32<7, 16>(a, num_sms, smem_optin, st)
+                   : launch_search_m32<7, 8>(a, num_sms, smem_optin, st);
+      if (small)
+        return r16 ? launch_search_m32<8, 16>(a, num_sms, smem_optin, st)
+                   : launch_search_m32<8, 8>(a, num_sms, smem_optin, st);
+      return r16 ? launch_search_m32<16, 16>(a, num_sms, smem_optin, st)
+                 : launch_search_m32<16, 8>(a, num_sms, smem_optin, st);
     case 2:
       return small ? launch_search_t<2, 8>(a, num_sms, smem_optin, st)
                    : launch_search_t<2, 16>(a, num_sms, smem_optin, st);
