@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--screen", default="bf16", choices=["bf16", "none"],
                     help="path timed for `value`; the other one is timed beside it")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the other path")
+    ap.add_argument("--autotune", action="store_true",
+                    help="run pg_autotune (launch shapes only; results unchanged) before timing")
     return ap.parse_args()
 
 
@@ -274,6 +276,11 @@ def run_ours(args):
     stream = torch.cuda.Stream(dev)
     h = pg.Handle(local, stream=stream)
     launches_per_build = 8 + 8 * params.link_rounds
+    tuning = None
+    if args.autotune:
+        t0 = time.perf_counter()
+        _, tun = h.autotune(base, gt, params)
+        tuning = dict(tun.as_dict(), seconds=round(time.perf_counter() - t0, 2))
     stats = []
     for _ in range(args.warmup):
         h.build_device(base, gt, graph, proj, params)
@@ -375,6 +382,7 @@ def run_ours(args):
                              "prune": [round(x, 2) for x in list(s.ms_prune)[:params.link_rounds]],
                              "merge": [round(x, 2) for x in list(s.ms_merge)[:params.link_rounds]]},
                 "screen": args.screen,
+                "tuning": tuning,
                 "rescored": list(s.rescored)[:params.link_rounds],
                 "other_path": other_line,
                 "gpu_launches": launches_per_build * args.steps,

@@ -27,8 +27,9 @@ _u64p = ctypes.POINTER(ctypes.c_uint64)
 
 def build(force: bool = False) -> str:
     lib = os.path.join(HERE, "_build", "libpg_oracle.so")
-    src = os.path.join(HERE, "pg_oracle.c")
-    if force or not os.path.exists(lib) or os.path.getmtime(lib) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("pg_oracle.c", "pg_oracle_roar.c")]
+    if force or not os.path.exists(lib) or any(os.path.getmtime(lib) < os.path.getmtime(s)
+                                               for s in srcs):
         subprocess.check_call([os.path.join(HERE, "build_oracle.sh")], stdout=subprocess.DEVNULL)
     return lib
 
@@ -69,6 +70,20 @@ def lib():
                                 ctypes.c_uint64, _u32p, _u32p, _u32p, ctypes.c_void_p]
         L.pgo_build.restype = ctypes.c_int
         L.pgo_num_threads.restype = ctypes.c_int
+        L.pgo_dist_avx.argtypes = [_f32p, _f32p, ctypes.c_uint64]
+        L.pgo_dist_avx.restype = ctypes.c_float
+        L.pgo_match_sup.argtypes = [_f32p, ctypes.c_uint64, ctypes.c_uint32, _u32p,
+                                    ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.c_uint32, _u64p, _u32p, ctypes.c_uint64]
+        L.pgo_match_sup.restype = ctypes.c_longlong
+        L.pgo_fusion_nn.argtypes = [_f32p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.c_uint32, _u64p, _u32p, _u64p, _u64p, _u32p,
+                                    ctypes.c_uint64]
+        L.pgo_fusion_nn.restype = ctypes.c_longlong
+        L.pgo_fusion_final.argtypes = [_f32p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
+                                       ctypes.c_uint32, ctypes.c_uint32, _u32p, _u64p, _u32p,
+                                       _u32p, _u64p, _u32p, ctypes.c_uint64]
+        L.pgo_fusion_final.restype = ctypes.c_longlong
         _LIB = L
     return _LIB
 
@@ -286,3 +301,61 @@ def split_lists(lists: np.ndarray, r: int, p: int):
     pruned_num = lists[:, 1 + r].copy()
     pruned = lists[:, 2 + r:2 + r + p].copy()
     return rev, rev_num, pruned, pruned_num
+
+
+# ---------------------------------------------------------------- CPU RoarGraph path (CSR graphs)
+def dist_avx(a, b) -> np.float32:
+    """compare (tests/test_t2iend.cu:31-80) in its AVX-512 FP32 order."""
+    a = _f32(a)
+    b = _f32(b)
+    return np.float32(lib().pgo_dist_avx(_p(a, _f32p), _p(b, _f32p), a.shape[0]))
+
+
+def _csr_out(cap: int, n: int):
+    return np.zeros(n + 1, dtype=np.uint64), np.zeros(max(cap, 1), dtype=np.uint32)
+
+
+def match_sup(base, gt, topn: int, m_nn: int = 40):
+    """MatchSup (tests/test_t2iend.cu:365-488) round `topn`: CSR (off, ids)."""
+    base = _f32(base)
+    gt = _u32(gt)
+    n, d = base.shape
+    off, ids = _csr_out(n * 128, n)
+    k = lib().pgo_match_sup(_p(base, _f32p), n, d, _p(gt, _u32p), gt.shape[0], gt.shape[1], topn,
+                            m_nn, _p(off, _u64p), _p(ids, _u32p), ids.shape[0])
+    assert k >= 0
+    return off, ids[:k].copy()
+
+
+def fusion_nn(base, rounds, m_nn: int = 40):
+    """FusionNN (tests/test_t2iend.cu:490-537) over supply graphs [(off, ids), ...]: CSR."""
+    base = _f32(base)
+    n, d = base.shape
+    sup_off = np.ascontiguousarray(np.concatenate([o for o, _ in rounds]), dtype=np.uint64)
+    sup_ids = _u32(np.concatenate([i for _, i in rounds]) if rounds else np.zeros(1, np.uint32))
+    sup_base = np.ascontiguousarray(np.cumsum([0] + [len(i) for _, i in rounds])[:-1],
+                                    dtype=np.uint64)
+    off, ids = _csr_out(n * 2 * m_nn, n)
+    k = lib().pgo_fusion_nn(_p(base, _f32p), n, d, m_nn, len(rounds), _p(sup_off, _u64p),
+                            _p(sup_ids, _u32p), _p(sup_base, _u64p), _p(off, _u64p),
+                            _p(ids, _u32p), ids.shape[0])
+    assert k >= 0
+    return off, ids[:k].copy()
+
+
+def fusion_final(base, supply, bip, link, m_final: int = 70):
+    """FusionFinal (tests/test_t2iend.cu:539-613): supply n x m_supply (projection), bip CSR
+    (FusionNN graph), link n x m_link (GPU graph): CSR."""
+    base = _f32(base)
+    supply = _u32(supply)
+    link = _u32(link)
+    n, d = base.shape
+    b_off = np.ascontiguousarray(bip[0], dtype=np.uint64)
+    b_ids = _u32(bip[1] if len(bip[1]) else np.zeros(1, np.uint32))
+    bmax = int(np.diff(b_off).max()) if n else 0
+    off, ids = _csr_out(n * (bmax + m_final), n)
+    k = lib().pgo_fusion_final(_p(base, _f32p), n, d, supply.shape[1], link.shape[1], m_final,
+                               _p(supply, _u32p), _p(b_off, _u64p), _p(b_ids, _u32p),
+                               _p(link, _u32p), _p(off, _u64p), _p(ids, _u32p), ids.shape[0])
+    assert k >= 0
+    return off, ids[:k].copy()

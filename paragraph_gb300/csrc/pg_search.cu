@@ -42,14 +42,17 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
       : "memory");
 }
 
+// try_wait with a suspend-time hint: a waiting warp sleeps until the phase completes (or the
+// hint, in ns, runs out) instead of spinning on the issue slots the other warps need.
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  constexpr uint32_t kSuspendNs = 100000;
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(kSuspendNs)
       : "memory");
   return ok != 0;
 }
@@ -609,9 +612,12 @@ __global__ void __launch_bounds__(32, KSTEPS <= 8 ? 20 : 12) k_search_m32(Search
       cand_key = pack_key(newc ? dist : FLT_MAX, 32u + lane);
       cand_id = node;
       // merge by rank: only scored candidates can enter the top (the others carry FLT_MAX and
-      // positions after every retained entry)
+      // positions after every retained entry), and of those only the ones below the current
+      // 32nd key: a candidate above it displaces nothing and lands at rank >= 32, and every
+      // candidate below an entering one enters too, so the ranks come out the same
+      const uint64_t worst = __shfl_sync(kFull, top_key, 31);
       uint32_t shift = 0, cpos = 0xFFFFFFFFu;
-      unsigned rem = scored;
+      unsigned rem = __ballot_sync(kFull, newc && cand_key < worst);
       while (rem) {
         const uint32_t c = static_cast<uint32_t>(__ffs(static_cast<int>(rem)) - 1);
         rem &= rem - 1u;
