@@ -91,7 +91,10 @@ typedef struct pg_stats {
   float ms_h2d, ms_d2h;      /* pg_build_host only */
   uint64_t h2d_bytes, d2h_bytes;
   uint32_t ep;               /* entry point (most frequent ground-truth id, MatchNN rule) */
-  uint32_t reserved[7];
+  float ms_match_sup;        /* pg_build_index: the MatchSup rounds */
+  float ms_fusion_nn;        /* pg_build_index: FusionNN */
+  float ms_fusion_final;     /* pg_build_index: FusionFinal */
+  uint32_t reserved[4];
 } pg_stats;
 
 typedef struct pg_handle_s* pg_handle;
@@ -144,6 +147,44 @@ int pg_build_batched_device(pg_handle h, const pg_params* p, const float* d_base
                             const uint32_t* d_gt, const uint64_t* node_off,
                             const uint64_t* query_off, uint32_t count, uint32_t* d_graph,
                             uint32_t* d_proj, pg_stats* st);
+
+/* ---- CPU RoarGraph path and final fusion (tests/test_t2iend.cu:365-613), on the GPU --------
+ * The reference runs these on the host beside its GPU build.  Results equal its one-thread run
+ * (distances in compare()'s AVX-512 FP32 order, lists sorted by (distance, id)), with MatchSup's
+ * reverse appends in ascending query order and short merged MatchSup lists in ascending id
+ * order (the reference writes std::unordered_set order there).  Lists are rows of a fixed stride
+ * with a count per row; D must be a multiple of 4.
+ *
+ * pg_match_sup: MatchSup (:365-488) round `topn` (1-based rank of the matched ground-truth id):
+ *   out n x m_nn, cnt n.  gt: q x gt_k, ids >= n end a row (the reference's padding).
+ * pg_fusion_nn: FusionNN (:490-537) over `rounds` MatchSup outputs (rounds x n x m_nn ids and
+ *   rounds x n counts, round order as the driver's :912-921); MatchNN's own graph is empty in the
+ *   reference (its graph-building loop is commented out, :234-306).  out n x 2*m_nn.
+ * pg_fusion_final: FusionFinal (:539-613).  Bipartite lists (the FusionNN graph) as CSR
+ *   (d_bip_off, n + 1 offsets) or as rows of bip_stride with counts (d_bip_off NULL); supply =
+ *   the projection (n x m_supply), link = the link graph (n x m_link).  Row i of out (stride
+ *   out_stride) holds the node's bipartite ids then its pruned ids; a row that does not fit makes
+ *   the call return PG_EUNSUPPORTED.
+ * pg_build_index: the reference driver's whole index (test_t2iend.cu:974-1229): the GPU build
+ *   (K0..K11), `match_rounds` MatchSup rounds (topn 1..match_rounds), FusionNN(m_nn) and
+ *   FusionFinal(m_supply = proj_degree, m_link = degree, m_final).  The driver's values are
+ *   match_rounds 6, m_nn 40, m_final 70; out_stride >= 2*m_nn + m_final.  The entry point is
+ *   pg_entry_point of the host ground truth. */
+int pg_match_sup(pg_handle h, const float* d_base, uint64_t n, uint32_t d, const uint32_t* d_gt,
+                 uint64_t q, uint32_t gt_k, uint32_t topn, uint32_t m_nn, uint32_t* d_out,
+                 uint32_t* d_cnt);
+int pg_fusion_nn(pg_handle h, const float* d_base, uint64_t n, uint32_t d, uint32_t rounds,
+                 const uint32_t* d_sup, const uint32_t* d_sup_cnt, uint32_t m_nn,
+                 uint32_t* d_out, uint32_t* d_cnt);
+int pg_fusion_final(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
+                    const uint64_t* d_bip_off, const uint32_t* d_bip_ids,
+                    const uint32_t* d_bip_cnt, uint32_t bip_stride, const uint32_t* d_supply,
+                    uint32_t m_supply, const uint32_t* d_link, uint32_t m_link, uint32_t m_final,
+                    uint32_t out_stride, uint32_t* d_out, uint32_t* d_cnt);
+int pg_build_index(pg_handle h, const pg_params* p, const float* d_base, uint64_t n, uint32_t d,
+                   const uint32_t* d_gt, uint64_t q, uint32_t match_rounds, uint32_t m_nn,
+                   uint32_t m_final, uint32_t out_stride, uint32_t* d_out, uint32_t* d_cnt,
+                   pg_stats* st);
 
 /* ---- autotuning (no counterpart in the reference: its launch shapes, beam width and hash
  * capacity are compile-time constants, tests/test_t2iend.cu:671-727) --------------------------

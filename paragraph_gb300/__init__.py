@@ -58,7 +58,8 @@ class Stats(ctypes.Structure):
                 ("ms_merge", ctypes.c_float * 4), ("ms_h2d", ctypes.c_float),
                 ("ms_d2h", ctypes.c_float), ("h2d_bytes", ctypes.c_uint64),
                 ("d2h_bytes", ctypes.c_uint64), ("ep", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 7)]
+                ("ms_match_sup", ctypes.c_float), ("ms_fusion_nn", ctypes.c_float),
+                ("ms_fusion_final", ctypes.c_float), ("reserved", ctypes.c_uint32 * 4)]
 
     def as_dict(self):
         out = {}
@@ -114,6 +115,12 @@ SIGNATURES = {
                                                 ctypes.c_int, _VP, _VP, _VP, _VP, _U64P]),
     "pg_query_search": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _U32, _VP, _U64, _U32, _U32,
                                        _U32, _U32, _U32, _U32, _U32, _VP, _U64P, _U64P]),
+    "pg_match_sup": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _U64, _U32, _U32, _U32, _VP, _VP]),
+    "pg_fusion_nn": (ctypes.c_int, [_VP, _VP, _U64, _U32, _U32, _VP, _VP, _U32, _VP, _VP]),
+    "pg_fusion_final": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _VP, _VP, _U32, _VP, _U32, _VP,
+                                       _U32, _U32, _U32, _VP, _VP]),
+    "pg_build_index": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _U64, _U32, _VP, _U64,
+                                      _U32, _U32, _U32, _U32, _VP, _VP, ctypes.POINTER(Stats)]),
     "pg_set_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
     "pg_get_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
     "pg_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _U32, _VP, _VP, _VP, _U32,
@@ -290,6 +297,45 @@ class Handle:
                                ctypes.byref(it)))
         return int(ev.value), int(it.value)
 
+
+    # ---- CPU RoarGraph path and final fusion (tests/test_t2iend.cu:365-613) on the GPU
+    def match_sup(self, base, gt, topn: int, out, cnt, m_nn: int = 40):
+        """pg_match_sup: MatchSup round `topn`; out n x m_nn, cnt n (device tensors)."""
+        n, d = base.shape
+        _check(lib().pg_match_sup(self._h, _ptr(base), n, d, _ptr(gt), gt.shape[0], gt.shape[1],
+                                  topn, m_nn, _ptr(out), _ptr(cnt)))
+
+    def fusion_nn(self, base, sup, sup_cnt, out, cnt, m_nn: int = 40):
+        """pg_fusion_nn over rounds x n x m_nn lists (sup) and rounds x n counts."""
+        n, d = base.shape
+        _check(lib().pg_fusion_nn(self._h, _ptr(base), n, d, sup.shape[0], _ptr(sup),
+                                  _ptr(sup_cnt), m_nn, _ptr(out), _ptr(cnt)))
+
+    def fusion_final(self, base, supply, link, out, cnt, bip_off=None, bip_ids=None,
+                     bip_rows=None, bip_cnt=None, m_final: int = 70):
+        """pg_fusion_final; bipartite lists as CSR (bip_off, bip_ids) or rows (bip_rows,
+        bip_cnt); out n x stride, cnt n."""
+        n, d = base.shape
+        if bip_off is not None:
+            ids, stride = bip_ids, 0
+        else:
+            ids, stride = bip_rows, bip_rows.shape[1]
+        _check(lib().pg_fusion_final(self._h, _ptr(base), n, d, _ptr(bip_off), _ptr(ids),
+                                     _ptr(bip_cnt), stride, _ptr(supply), supply.shape[1],
+                                     _ptr(link), link.shape[1], m_final, out.shape[1], _ptr(out),
+                                     _ptr(cnt)))
+
+    def build_index(self, base, gt, out, cnt, params: Params | None = None,
+                    match_rounds: int = 6, m_nn: int = 40, m_final: int = 70) -> Stats:
+        """pg_build_index: the driver's whole index (GPU build + MatchSup rounds + FusionNN +
+        FusionFinal); out n x stride (>= 2*m_nn + m_final), cnt n."""
+        params = params or default_params()
+        n, d = base.shape
+        st = Stats()
+        _check(lib().pg_build_index(self._h, ctypes.byref(params), _ptr(base), n, d, _ptr(gt),
+                                    gt.shape[0], match_rounds, m_nn, m_final, out.shape[1],
+                                    _ptr(out), _ptr(cnt), ctypes.byref(st)))
+        return st
 
     def set_tuning(self, tuning: Tuning):
         _check(lib().pg_set_tuning(self._h, ctypes.byref(tuning)))

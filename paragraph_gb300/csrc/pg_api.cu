@@ -137,6 +137,8 @@ struct pg_handle_s {
   cudaGraphExec_t gexec = nullptr;  // captured build (PG_FLAG_CUDA_GRAPH) and what it was built for
   GraphKey gkey;
   pg_tuning tune{};  // launch shapes of later builds (zero = defaults)
+  char* ws2 = nullptr;  // pg_build_index: graphs that outlive one stage (projection, link, rounds)
+  size_t ws2_bytes = 0;
   std::mutex mu;
 };
 
@@ -239,6 +241,7 @@ int status_to_error(uint32_t s) {
   if (s & 4u) return fail(PG_EINVAL, "input holds an id >= n that is not tomb (status 0x%x)", s);
   if (s & 1u) return fail(PG_ETIMEOUT, "a search exceeded max_search_iters (status 0x%x)", s);
   if (s & 2u) return fail(PG_ETIMEOUT, "a bounded device wait gave up (status 0x%x)", s);
+  if (s & 8u) return fail(PG_EUNSUPPORTED, "a list exceeded the capacity of a kernel (status 0x%x)", s);
   if (s) return fail(PG_ECUDA, "device status 0x%x", s);
   return PG_OK;
 }
@@ -509,6 +512,120 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
   return PG_OK;
 }
 
+
+// ---- CPU RoarGraph path (pg_roar.cu) ------------------------------------------------------
+
+int ensure_ws2(pg_handle h, size_t bytes) {
+  if (bytes <= h->ws2_bytes) return PG_OK;
+  if (h->ws2) cudaFree(h->ws2);
+  h->ws2 = nullptr;
+  h->ws2_bytes = 0;
+  cudaError_t e = cudaMalloc(&h->ws2, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(PG_ENOMEM, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+  }
+  h->ws2_bytes = bytes;
+  return PG_OK;
+}
+
+struct SupLayout {
+  size_t claim, plist, pcnt, indeg, offs, tiles, cursor, edges, rev, rnum, total;
+};
+
+SupLayout sup_layout(uint64_t n, uint64_t q, uint32_t m_nn) {
+  SupLayout l{};
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = o;
+    o += align_up(bytes);
+    return at;
+  };
+  const uint32_t maxdeg = 128 - m_nn;
+  l.claim = take(n * 4);
+  l.plist = take(q * m_nn * 4);
+  l.pcnt = take(q * 4);
+  l.indeg = take(n * 4);
+  l.offs = take((n + 1) * 4);
+  l.tiles = take(((n + pg::kScanTileElems - 1) / pg::kScanTileElems + 1) * 4);
+  l.cursor = take(n * 4);
+  l.edges = take(q * m_nn * 4);
+  l.rev = take(n * maxdeg * 4);
+  l.rnum = take(n * 4);
+  l.total = o;
+  return l;
+}
+
+int check_sup(uint64_t n, uint32_t d, uint64_t q, uint32_t gt_k, uint32_t topn, uint32_t m_nn) {
+  if (n == 0 || n >= 0x7FFFFFFFull || q == 0 || q >= 0x7FFFFFFFull)
+    return fail(PG_EINVAL, "n and q must be in [1, 2^31-1)");
+  if (d == 0 || d % 4 != 0) return fail(PG_EUNSUPPORTED, "d=%u must be a positive multiple of 4", d);
+  if (gt_k == 0 || gt_k > pg::roar_capacity()) return fail(PG_EINVAL, "gt_k must be in [1, 256]");
+  if (topn >= gt_k) return fail(PG_EINVAL, "topn=%u must be < gt_k=%u", topn, gt_k);
+  if (m_nn < 1 || m_nn > 64) return fail(PG_EINVAL, "m_nn=%u must be in [1, 64]", m_nn);
+  return PG_OK;
+}
+
+// One MatchSup round on the handle's stream (caller holds the lock; no synchronisation).
+int enqueue_match_sup(pg_handle h, const float* base, uint64_t n, uint32_t d, const uint32_t* gt,
+                      uint64_t q, uint32_t gt_k, uint32_t topn, uint32_t m_nn, uint32_t* out,
+                      uint32_t* cnt) {
+  const SupLayout lay = sup_layout(n, q, m_nn);
+  int rc = ensure_ws(h, lay.total);
+  if (rc) return rc;
+  cudaStream_t s = h->stream;
+  char* w = h->ws;
+  pg::SupArgs a{};
+  a.base = base;
+  a.n = n;
+  a.d = d;
+  a.gt = gt;
+  a.q = q;
+  a.gt_k = gt_k;
+  a.topn = topn;
+  a.m_nn = m_nn;
+  a.maxdeg = 128 - m_nn;
+  uint32_t* claim = reinterpret_cast<uint32_t*>(w + lay.claim);
+  a.claim = claim;
+  a.plist = reinterpret_cast<uint32_t*>(w + lay.plist);
+  a.pcnt = reinterpret_cast<uint32_t*>(w + lay.pcnt);
+  a.indeg = reinterpret_cast<uint32_t*>(w + lay.indeg);
+  uint32_t* offs = reinterpret_cast<uint32_t*>(w + lay.offs);
+  uint32_t* rev = reinterpret_cast<uint32_t*>(w + lay.rev);
+  uint32_t* rnum = reinterpret_cast<uint32_t*>(w + lay.rnum);
+  a.rev = rev;
+  a.rnum = rnum;
+  a.out = out;
+  a.cnt = cnt;
+  a.status = h->d_status;
+  PG_CUDA(pg::launch_sup_claim(gt, q, gt_k, topn, n, claim, h->num_sms, s));
+  PG_CUDA(cudaMemsetAsync(a.indeg, 0, n * 4, s));
+  PG_CUDA(pg::launch_sup_prune(a, h->num_sms, s));
+  PG_CUDA(pg::launch_reverse_csr(a.plist, a.pcnt, m_nn, n, a.indeg, offs,
+                                 reinterpret_cast<uint32_t*>(w + lay.tiles),
+                                 reinterpret_cast<uint32_t*>(w + lay.cursor),
+                                 reinterpret_cast<uint32_t*>(w + lay.edges), h->num_sms, s, q));
+  PG_CUDA(pg::launch_reverse_lists(offs, reinterpret_cast<uint32_t*>(w + lay.edges), n, a.maxdeg,
+                                   rev, rnum, h->num_sms, s));
+  PG_CUDA(pg::launch_sup_merge(a, h->num_sms, s));
+  return PG_OK;
+}
+
+int finish(pg_handle h) {
+  PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, h->stream));
+  PG_CUDA(cudaStreamSynchronize(h->stream));
+  return status_to_error(*h->h_status);
+}
+
+pg::FusionArgs fusion_args(pg_handle h, const float* base, uint64_t n, uint32_t d) {
+  pg::FusionArgs a{};
+  a.base = base;
+  a.n = n;
+  a.d = d;
+  a.status = h->d_status;
+  return a;
+}
+
 // pg_query_search without taking the handle's lock (callers hold it).
 int query_search_locked(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
                         const uint32_t* d_graph, uint32_t graph_degree, const float* d_queries,
@@ -627,6 +744,7 @@ int pg_destroy(pg_handle h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   cudaFree(h->ws);
+  cudaFree(h->ws2);
   cudaFree(h->inbuf);
   cudaFree(h->d_status);
   cudaFree(h->d_counters);
@@ -1122,6 +1240,170 @@ int pg_autotune(pg_handle h, pg_params* p, const float* d_base, uint32_t d, cons
   }
   p->km = tp.km;
   if (out) *out = best;
+  return PG_OK;
+}
+
+// ---------------------------------------------------------------- CPU RoarGraph path
+
+int pg_match_sup(pg_handle h, const float* d_base, uint64_t n, uint32_t d, const uint32_t* d_gt,
+                 uint64_t q, uint32_t gt_k, uint32_t topn, uint32_t m_nn, uint32_t* d_out,
+                 uint32_t* d_cnt) {
+  if (!h || !d_base || !d_gt || !d_out || !d_cnt) return fail(PG_EINVAL, "NULL argument");
+  int rc = check_sup(n, d, q, gt_k, topn, m_nn);
+  if (rc) return rc;
+  if (!aligned16(d_base)) return fail(PG_EINVAL, "base must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, h->stream));
+  rc = enqueue_match_sup(h, d_base, n, d, d_gt, q, gt_k, topn, m_nn, d_out, d_cnt);
+  if (rc) return rc;
+  return finish(h);
+}
+
+int pg_fusion_nn(pg_handle h, const float* d_base, uint64_t n, uint32_t d, uint32_t rounds,
+                 const uint32_t* d_sup, const uint32_t* d_sup_cnt, uint32_t m_nn,
+                 uint32_t* d_out, uint32_t* d_cnt) {
+  if (!h || !d_base || !d_sup || !d_sup_cnt || !d_out || !d_cnt)
+    return fail(PG_EINVAL, "NULL argument");
+  if (n == 0 || n >= 0x7FFFFFFFull) return fail(PG_EINVAL, "bad n");
+  if (d == 0 || d % 4 != 0) return fail(PG_EUNSUPPORTED, "d must be a positive multiple of 4");
+  if (m_nn < 1 || m_nn > 64) return fail(PG_EINVAL, "m_nn must be in [1, 64]");
+  if (rounds < 1 || rounds * m_nn > pg::roar_capacity())
+    return fail(PG_EUNSUPPORTED, "rounds * m_nn must be in [1, %u]", pg::roar_capacity());
+  if (!aligned16(d_base)) return fail(PG_EINVAL, "base must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, h->stream));
+  pg::FusionArgs a = fusion_args(h, d_base, n, d);
+  a.sup = d_sup;
+  a.sup_cnt = d_sup_cnt;
+  a.sup_stride = m_nn;
+  a.rounds = rounds;
+  a.m_out = 2 * m_nn;
+  a.out = d_out;
+  a.cnt = d_cnt;
+  a.out_stride = 2 * m_nn;
+  PG_CUDA(pg::launch_fusion_nn(a, h->num_sms, h->stream));
+  return finish(h);
+}
+
+int pg_fusion_final(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
+                    const uint64_t* d_bip_off, const uint32_t* d_bip_ids,
+                    const uint32_t* d_bip_cnt, uint32_t bip_stride, const uint32_t* d_supply,
+                    uint32_t m_supply, const uint32_t* d_link, uint32_t m_link, uint32_t m_final,
+                    uint32_t out_stride, uint32_t* d_out, uint32_t* d_cnt) {
+  if (!h || !d_base || !d_bip_ids || !d_supply || !d_link || !d_out || !d_cnt)
+    return fail(PG_EINVAL, "NULL argument");
+  if (!d_bip_off && !d_bip_cnt) return fail(PG_EINVAL, "bipartite lists need offsets or counts");
+  if (n == 0 || n >= 0x7FFFFFFFull) return fail(PG_EINVAL, "bad n");
+  if (d == 0 || d % 4 != 0) return fail(PG_EUNSUPPORTED, "d must be a positive multiple of 4");
+  if (m_final < 1 || m_final > 128) return fail(PG_EINVAL, "m_final must be in [1, 128]");
+  if (m_link + m_supply > pg::roar_capacity())
+    return fail(PG_EUNSUPPORTED, "m_link + m_supply must be <= %u", pg::roar_capacity());
+  if (!aligned16(d_base)) return fail(PG_EINVAL, "base must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, h->stream));
+  pg::FusionArgs a = fusion_args(h, d_base, n, d);
+  a.bip = d_bip_ids;
+  a.bip_off = d_bip_off;
+  a.bip_cnt = d_bip_cnt;
+  a.bip_stride = bip_stride;
+  a.supply = d_supply;
+  a.m_supply = m_supply;
+  a.link = d_link;
+  a.m_link = m_link;
+  a.m_out = m_final;
+  a.out = d_out;
+  a.cnt = d_cnt;
+  a.out_stride = out_stride;
+  PG_CUDA(pg::launch_fusion_final(a, h->num_sms, h->stream));
+  return finish(h);
+}
+
+int pg_build_index(pg_handle h, const pg_params* p, const float* d_base, uint64_t n, uint32_t d,
+                   const uint32_t* d_gt, uint64_t q, uint32_t match_rounds, uint32_t m_nn,
+                   uint32_t m_final, uint32_t out_stride, uint32_t* d_out, uint32_t* d_cnt,
+                   pg_stats* st) {
+  if (!h) return fail(PG_EINVAL, "handle is NULL");
+  int rc = check_params(p, n, d, q);
+  if (rc) return rc;
+  if (p->link_rounds == 0) return fail(PG_EINVAL, "the index needs the link graph (link_rounds > 0)");
+  if (!d_base || !d_gt || !d_out || !d_cnt) return fail(PG_EINVAL, "NULL argument");
+  if (match_rounds < 1 || match_rounds >= p->gt_k)
+    return fail(PG_EINVAL, "match_rounds must be in [1, gt_k)");
+  rc = check_sup(n, d, q, p->gt_k, match_rounds, m_nn);
+  if (rc) return rc;
+  if (match_rounds * m_nn > pg::roar_capacity() || 2 * m_nn + p->degree + p->proj_degree >
+                                                          pg::roar_capacity())
+    return fail(PG_EUNSUPPORTED, "match_rounds * m_nn and 2*m_nn + degree + 16 must be <= %u",
+                pg::roar_capacity());
+  if (m_final < 1 || m_final > 128) return fail(PG_EINVAL, "m_final must be in [1, 128]");
+  if (out_stride < 2 * m_nn + m_final)
+    return fail(PG_EINVAL, "out_stride must be >= 2*m_nn + m_final = %u", 2 * m_nn + m_final);
+  if (!aligned16(d_base)) return fail(PG_EINVAL, "base must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  if (st) std::memset(st, 0, sizeof(*st));
+  // graphs that outlive a stage: link graph, projection, the rounds' lists, FusionNN's lists
+  const size_t b_link = align_up(n * p->degree * 4), b_proj = align_up(n * p->proj_degree * 4);
+  const size_t b_sup = align_up(static_cast<size_t>(match_rounds) * n * m_nn * 4);
+  const size_t b_supc = align_up(static_cast<size_t>(match_rounds) * n * 4);
+  const size_t b_fnn = align_up(n * 2 * m_nn * 4), b_fnnc = align_up(n * 4);
+  rc = ensure_ws2(h, b_link + b_proj + b_sup + b_supc + b_fnn + b_fnnc);
+  if (rc) return rc;
+  uint32_t* link = reinterpret_cast<uint32_t*>(h->ws2);
+  uint32_t* proj = reinterpret_cast<uint32_t*>(h->ws2 + b_link);
+  uint32_t* sup = reinterpret_cast<uint32_t*>(h->ws2 + b_link + b_proj);
+  uint32_t* supc = reinterpret_cast<uint32_t*>(h->ws2 + b_link + b_proj + b_sup);
+  uint32_t* fnn = reinterpret_cast<uint32_t*>(h->ws2 + b_link + b_proj + b_sup + b_supc);
+  uint32_t* fnnc = reinterpret_cast<uint32_t*>(h->ws2 + b_link + b_proj + b_sup + b_supc + b_fnn);
+  pg_params bp = *p;
+  bp.flags &= ~PG_FLAG_CUDA_GRAPH;
+  rc = run_build(h, &bp, d_base, n, d, d_gt, q, link, proj, st);  // K0..K11 (synchronises)
+  if (rc) return rc;
+  cudaStream_t s = h->stream;
+  PG_CUDA(cudaEventRecord(h->ev[10], s));
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, s));
+  for (uint32_t r = 0; r < match_rounds; r++) {  // MatchSup rounds topn = 1 .. match_rounds
+    rc = enqueue_match_sup(h, d_base, n, d, d_gt, q, p->gt_k, r + 1, m_nn,
+                           sup + static_cast<size_t>(r) * n * m_nn, supc + static_cast<size_t>(r) * n);
+    if (rc) return rc;
+  }
+  PG_CUDA(cudaEventRecord(h->ev[11], s));
+  pg::FusionArgs a = fusion_args(h, d_base, n, d);
+  a.sup = sup;
+  a.sup_cnt = supc;
+  a.sup_stride = m_nn;
+  a.rounds = match_rounds;
+  a.m_out = 2 * m_nn;
+  a.out = fnn;
+  a.cnt = fnnc;
+  a.out_stride = 2 * m_nn;
+  PG_CUDA(pg::launch_fusion_nn(a, h->num_sms, s));
+  PG_CUDA(cudaEventRecord(h->ev[12], s));
+  pg::FusionArgs f = fusion_args(h, d_base, n, d);
+  f.bip = fnn;
+  f.bip_cnt = fnnc;
+  f.bip_stride = 2 * m_nn;
+  f.supply = proj;
+  f.m_supply = p->proj_degree;
+  f.link = link;
+  f.m_link = p->degree;
+  f.m_out = m_final;
+  f.out = d_out;
+  f.cnt = d_cnt;
+  f.out_stride = out_stride;
+  PG_CUDA(pg::launch_fusion_final(f, h->num_sms, s));
+  PG_CUDA(cudaEventRecord(h->ev[13], s));
+  rc = finish(h);
+  if (rc) return rc;
+  if (st) {
+    PG_CUDA(cudaEventElapsedTime(&st->ms_match_sup, h->ev[10], h->ev[11]));
+    PG_CUDA(cudaEventElapsedTime(&st->ms_fusion_nn, h->ev[11], h->ev[12]));
+    PG_CUDA(cudaEventElapsedTime(&st->ms_fusion_final, h->ev[12], h->ev[13]));
+    st->ms_total += st->ms_match_sup + st->ms_fusion_nn + st->ms_fusion_final;
+  }
   return PG_OK;
 }
 

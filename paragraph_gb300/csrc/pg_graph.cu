@@ -361,10 +361,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const uint32_t* __r
 // Every kept edge b -> p becomes the entry b in p's CSR segment (order fixed later by sorting).
 __global__ void k_scatter_reverse(const uint32_t* __restrict__ pruned,
                                   const uint32_t* __restrict__ pruned_num, uint32_t p_len,
-                                  uint64_t n, const uint32_t* __restrict__ offs,
+                                  uint64_t rows, const uint32_t* __restrict__ offs,
                                   uint32_t* __restrict__ cursor, uint32_t* __restrict__ edges) {
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-  for (uint64_t b = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; b < n;
+  for (uint64_t b = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; b < rows;
        b += stride) {
     const uint32_t cnt = pruned_num[b];
     for (uint32_t t = 0; t < cnt; t++) {
@@ -602,15 +602,16 @@ cudaError_t launch_prune_reverse(const PruneArgs& a, bool phase1, int num_sms, c
 cudaError_t launch_reverse_csr(const uint32_t* pruned, const uint32_t* pruned_num, uint32_t p_len,
                                uint64_t n, const uint32_t* indeg, uint32_t* offs,
                                uint32_t* tile_sums, uint32_t* cursor, uint32_t* edges,
-                               int num_sms, cudaStream_t st) {
+                               int num_sms, cudaStream_t st, uint64_t rows) {
+  if (rows == 0) rows = n;
   const uint32_t tiles = static_cast<uint32_t>((n + kScanTile - 1) / kScanTile);
   k_scan_tiles<<<tiles, kScanThreads, 0, st>>>(indeg, n, tile_sums);
   k_scan_tile_sums<<<1, kScanThreads, 0, st>>>(tile_sums, tiles, offs + n);
   k_scan_apply<<<tiles, kScanThreads, 0, st>>>(indeg, n, tile_sums, offs);
   cudaError_t e = cudaMemsetAsync(cursor, 0, n * sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
-  k_scatter_reverse<<<grid_for(n, 256, num_sms, 8), 256, 0, st>>>(pruned, pruned_num, p_len, n,
-                                                                   offs, cursor, edges);
+  k_scatter_reverse<<<grid_for(rows, 256, num_sms, 8), 256, 0, st>>>(pruned, pruned_num, p_len,
+                                                                      rows, offs, cursor, edges);
   return cudaGetLastError();
 }
 

@@ -78,6 +78,58 @@ struct SearchArgs {
   uint32_t max_blocks_per_sm;
 };
 
+// CPU RoarGraph path on the GPU (tests/test_t2iend.cu:365-613), pg_roar.cu.
+struct SupArgs {  // one MatchSup round
+  const float* base;
+  uint64_t n;
+  uint32_t d;
+  const uint32_t* gt;  // q x gt_k
+  uint64_t q;
+  uint32_t gt_k, topn, m_nn, maxdeg;  // maxdeg = 128 - m_nn reverse sources kept per base
+  const uint32_t* claim;  // n: lowest query whose gt[topn] is the base, or tomb
+  uint32_t* plist;        // q x m_nn: a matched query's pruned list
+  uint32_t* pcnt;         // q
+  uint32_t* indeg;        // n: reverse in-degree
+  const uint32_t* rev;    // n x maxdeg: first reverse sources (query indices, ascending)
+  const uint32_t* rnum;   // n
+  uint32_t* out;          // n x m_nn
+  uint32_t* cnt;          // n
+  uint32_t* status;
+};
+
+struct FusionArgs {
+  const float* base;
+  uint64_t n;
+  uint32_t d;
+  // FusionNN: `rounds` supply graphs, rounds x n x sup_stride ids + rounds x n counts
+  const uint32_t* sup;
+  const uint32_t* sup_cnt;
+  uint32_t sup_stride, rounds;
+  // FusionFinal: bipartite lists as CSR (bip_off != NULL) or rows of bip_stride with counts
+  const uint32_t* bip;
+  const uint64_t* bip_off;
+  const uint32_t* bip_cnt;
+  uint32_t bip_stride;
+  const uint32_t* supply;  // n x m_supply (projection)
+  uint32_t m_supply;
+  const uint32_t* link;  // n x m_link (link graph)
+  uint32_t m_link;
+  uint32_t m_out;  // prune width: 2*M_nn (FusionNN) or M_final
+  uint32_t* out;   // n x out_stride
+  uint32_t* cnt;   // n
+  uint32_t out_stride;
+  uint32_t* status;
+};
+
+bool roar_supported(uint32_t d, uint32_t m);
+uint32_t roar_capacity();
+cudaError_t launch_sup_claim(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint32_t topn,
+                             uint64_t n, uint32_t* claim, int num_sms, cudaStream_t st);
+cudaError_t launch_sup_prune(const SupArgs& a, int num_sms, cudaStream_t st);
+cudaError_t launch_sup_merge(const SupArgs& a, int num_sms, cudaStream_t st);
+cudaError_t launch_fusion_nn(const FusionArgs& a, int num_sms, cudaStream_t st);
+cudaError_t launch_fusion_final(const FusionArgs& a, int num_sms, cudaStream_t st);
+
 cudaError_t launch_match_winner(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint64_t n,
                                 uint32_t* winner, uint32_t* status, int num_sms, cudaStream_t st,
                                 const uint64_t* seg_off = nullptr,
@@ -91,10 +143,12 @@ cudaError_t launch_match_rows(const uint32_t* gt, uint32_t gt_k, uint64_t n,
 cudaError_t launch_validate_ids(const uint32_t* ids, uint64_t count, uint64_t n,
                                 uint32_t* status, int num_sms, cudaStream_t st);
 cudaError_t launch_prune_reverse(const PruneArgs& a, bool phase1, int num_sms, cudaStream_t st);
+// Reverse edges as CSR over n destinations: offs = exclusive scan of indeg, edges grouped by
+// destination holding the source row index.  `rows` pruned rows are scanned (0 = n).
 cudaError_t launch_reverse_csr(const uint32_t* pruned, const uint32_t* pruned_num, uint32_t p_len,
                                uint64_t n, const uint32_t* indeg, uint32_t* offs,
                                uint32_t* tile_sums, uint32_t* cursor, uint32_t* edges,
-                               int num_sms, cudaStream_t st);
+                               int num_sms, cudaStream_t st, uint64_t rows = 0);
 cudaError_t launch_reverse_lists(const uint32_t* offs, const uint32_t* edges, uint64_t n,
                                  uint32_t r, uint32_t* rev, uint32_t* rev_num, int num_sms,
                                  cudaStream_t st);
