@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--screen", default="bf16", choices=["bf16", "none"],
                     help="path timed for `value`; the other one is timed beside it")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the other path")
+    ap.add_argument("--no-index", action="store_true",
+                    help="skip timing the whole index (pg_build_index: build + RoarGraph path + "
+                         "FusionFinal)")
     ap.add_argument("--autotune", action="store_true",
                     help="run pg_autotune (launch shapes only; results unchanged) before timing")
     return ap.parse_args()
@@ -200,7 +203,7 @@ def cpu_baseline_sample(args, base_np, gt_np, seconds):
         dt = time.perf_counter() - t0
         ev = full["stats"]["evals_total"]
         desc = f"oracle full build (K0-K11) of all {args.n} points: {ev} evals in {dt:.1f} s"
-        return ev / dt, desc, oracle.num_threads()
+        return ev / dt, desc, oracle.num_threads(), full
     per_q = (t2 - t1) / pilot
     q_more = int(min(args.n - pilot, max(seconds - (t2 - t0), 0.0) / max(per_q, 1e-9)))
     sev2 = 0
@@ -211,7 +214,7 @@ def cpu_baseline_sample(args, base_np, gt_np, seconds):
     ev = p1["stats"]["evals_proj_prune"] + p1["stats"]["evals_proj_merge"] + pev + sev2
     desc = (f"oracle phase 1 (K0-K3) over all {args.n} points + round-1 search for "
             f"{pilot + q_more} queries: {ev} evals in {t3 - t0:.1f} s")
-    return ev / (t3 - t0), desc, oracle.num_threads()
+    return ev / (t3 - t0), desc, oracle.num_threads(), None
 
 
 def run_reference(args):
@@ -237,7 +240,7 @@ def run_reference(args):
     steps = max(args.steps, 1)
     per_step = max(min(args.cpu_seconds, 120.0 / (steps + args.warmup)), 3.0)
     for i in range(args.warmup + steps):
-        v, desc, threads = cpu_baseline_sample(args, base_np, gt_np, per_step)
+        v, desc, threads, _ = cpu_baseline_sample(args, base_np, gt_np, per_step)
         if i >= args.warmup:
             vals.append(v)
     value = statistics.mean(vals)
@@ -322,6 +325,25 @@ def run_ours(args):
                       "identical_edges": bool(torch.equal(graph, graph2) and torch.equal(proj, proj2)),
                       "speedup_of_timed_path": round(oms / (ms_total / args.steps), 3)}
         del graph2, proj2
+    # the driver's whole index: this build plus the CPU RoarGraph path (six MatchSup rounds,
+    # FusionNN) and FusionFinal, all on the GPU (pg_build_index)
+    index_line = None
+    if not args.no_index:
+        iout = torch.empty((n, 2 * 40 + 70), dtype=torch.int32, device=dev)
+        icnt = torch.empty((n,), dtype=torch.int32, device=dev)
+        h.build_index(base, gt, iout, icnt, params)
+        ist = [h.build_index(base, gt, iout, icnt, params) for _ in range(max(1, min(args.steps, 3)))]
+        last = ist[-1]
+        kk = icnt.float()
+        index_line = {"ms_per_index": round(statistics.mean(x.ms_total for x in ist), 3),
+                      "ms_gpu_build": round(last.ms_total - last.ms_match_sup - last.ms_fusion_nn
+                                            - last.ms_fusion_final, 3),
+                      "ms_match_sup_6_rounds": round(last.ms_match_sup, 3),
+                      "ms_fusion_nn": round(last.ms_fusion_nn, 3),
+                      "ms_fusion_final": round(last.ms_fusion_final, 3),
+                      "mean_degree": round(float(kk.mean()), 3), "max_degree": int(kk.max()),
+                      "params": "match_rounds 6, M_nn 40, M_final 70 (tests/test_t2iend.cu)"}
+        del iout, icnt
     evals = stats[-1].evals_total
     assert all(s.evals_total == evals for s in stats), "evaluation count changed between builds"
     value = evals * args.steps * world / (ms_total / 1e3)
@@ -360,8 +382,16 @@ def run_ours(args):
     roof = search_roofline(stats[-1], args, peak, peak_kind, params.link_rounds)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, desc, threads = cpu_baseline_sample(args, base_np, gt_np, args.cpu_seconds)
+        v, desc, threads, full = cpu_baseline_sample(args, base_np, gt_np, args.cpu_seconds)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
+        if index_line is not None and full is not None:
+            import oracle
+            t0 = time.perf_counter()
+            rounds = [oracle.match_sup(base_np, gt_np, r) for r in range(1, 7)]
+            fnn = oracle.fusion_nn(base_np, rounds)
+            oracle.fusion_final(base_np, full["proj"], fnn, full["graph"])
+            index_line["cpu_oracle_roar_s"] = round(time.perf_counter() - t0, 2)
+            index_line["cpu_oracle_cores"] = threads
     s = stats[-1]
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -385,6 +415,7 @@ def run_ours(args):
                 "tuning": tuning,
                 "rescored": list(s.rescored)[:params.link_rounds],
                 "other_path": other_line,
+                "index": index_line,
                 "gpu_launches": launches_per_build * args.steps,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary()}

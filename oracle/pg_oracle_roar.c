@@ -126,8 +126,23 @@ static int cmp_u32(const void* a, const void* b) {
   return x < y ? -1 : x > y;
 }
 
+/* Rows (stride, counts) -> CSR; returns the id count or -1 when cap is too small. */
+static long long compact_rows(const uint32_t* rows, const uint32_t* cnt, uint64_t stride,
+                              uint64_t n, uint64_t* off, uint32_t* ids, uint64_t cap) {
+  uint64_t o = 0;
+  for (uint64_t b = 0; b < n; b++) {
+    off[b] = o;
+    if (o + cnt[b] > cap) return -1;
+    memcpy(ids + o, rows + b * stride, sizeof(uint32_t) * cnt[b]);
+    o += cnt[b];
+  }
+  off[n] = o;
+  return (long long)o;
+}
+
 /* MatchSup (:365-488) for round topn.  gt: q x n_ctr.  Output CSR (off: n + 1; ids: capacity
- * cap).  Returns the number of ids written, or -1 when cap is too small. */
+ * cap).  Returns the number of ids written, or -1 when cap is too small.  The per-query prunes
+ * and per-base merges run in parallel; the reverse appends run in ascending query order. */
 long long pgo_match_sup(const float* base, uint64_t n, uint32_t d, const uint32_t* gt,
                         uint64_t q, uint32_t n_ctr, uint32_t topn, uint32_t m_nn, uint64_t* off,
                         uint32_t* ids, uint64_t cap) {
@@ -142,29 +157,40 @@ long long pgo_match_sup(const float* base, uint64_t n, uint32_t d, const uint32_
     claimed[nn] = 1;
     match[qi] = nn;
   }
+  uint32_t* qlist = (uint32_t*)malloc(sizeof(uint32_t) * q * m_nn); /* per query */
+  uint32_t* qcnt = (uint32_t*)calloc(q, sizeof(uint32_t));
+#pragma omp parallel
+  {
+    float dist[256];
+    uint32_t cid[256];
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t qi = 0; qi < (int64_t)q; qi++) { /* :407-430 */
+      const uint32_t cur = match[qi];
+      if (cur >= n) continue;
+      uint32_t c = 0;
+      for (uint32_t j = 0; j < n_ctr; j++) {
+        const uint32_t b = gt[(uint64_t)qi * n_ctr + j];
+        if (b >= n) break;
+        if (b == cur || contains(cid, c, b)) continue;
+        cid[c] = b;
+        dist[c] = dist_avx(base + (uint64_t)b * d, base + (uint64_t)cur * d, d);
+        c++;
+      }
+      sort_nb(dist, cid, c);
+      qcnt[qi] = rng_prune(base, d, n, m_nn, dist, cid, c, cur, 0,
+                           qlist + (uint64_t)qi * m_nn);
+    }
+  }
   uint32_t* plist = (uint32_t*)malloc(sizeof(uint32_t) * n * m_nn); /* match_graph rows */
   uint32_t* pcnt = (uint32_t*)calloc(n, sizeof(uint32_t));
   uint32_t* tmp = (uint32_t*)malloc(sizeof(uint32_t) * n * maxdeg);
   uint32_t* deg = (uint32_t*)calloc(n, sizeof(uint32_t));
   uint8_t* full = (uint8_t*)calloc(n, 1);
-  float* dist = (float*)malloc(sizeof(float) * 256);
-  uint32_t* cid = (uint32_t*)malloc(sizeof(uint32_t) * 256);
-  uint32_t res[128];
-  for (uint64_t qi = 0; qi < q; qi++) { /* :407-441, ascending query order */
+  for (uint64_t qi = 0; qi < q; qi++) { /* :431-440, ascending query order */
     const uint32_t cur = match[qi];
     if (cur >= n) continue;
-    uint32_t c = 0;
-    for (uint32_t j = 0; j < n_ctr; j++) {
-      const uint32_t b = gt[qi * n_ctr + j];
-      if (b >= n) break;
-      if (b == cur || contains(cid, c, b)) continue;
-      cid[c] = b;
-      dist[c] = dist_avx(base + (uint64_t)b * d, base + (uint64_t)cur * d, d);
-      c++;
-    }
-    sort_nb(dist, cid, c);
-    const uint32_t k = rng_prune(base, d, n, m_nn, dist, cid, c, cur, 0, res);
-    for (uint32_t i = 0; i < k; i++) {
+    const uint32_t* res = qlist + qi * m_nn;
+    for (uint32_t i = 0; i < qcnt[qi]; i++) {
       const uint32_t des = res[i];
       if (full[des]) continue;
       const uint32_t cd = deg[des]++;
@@ -173,58 +199,55 @@ long long pgo_match_sup(const float* base, uint64_t n, uint32_t d, const uint32_
       else if (cd == maxdeg)
         full[des] = 1;
     }
-    memcpy(plist + (uint64_t)cur * m_nn, res, sizeof(uint32_t) * k);
-    pcnt[cur] = k;
+    memcpy(plist + (uint64_t)cur * m_nn, res, sizeof(uint32_t) * qcnt[qi]);
+    pcnt[cur] = qcnt[qi];
   }
-  uint64_t o = 0;
-  long long ret = 0;
-  uint32_t* merged = (uint32_t*)malloc(sizeof(uint32_t) * (m_nn + maxdeg));
-  for (uint64_t b = 0; b < n && ret == 0; b++) { /* :449-475 */
-    uint32_t c = 0;
-    for (uint32_t i = 0; i < pcnt[b]; i++) {
-      const uint32_t x = plist[b * m_nn + i];
-      if (!contains(merged, c, x)) merged[c++] = x;
-    }
-    const uint32_t a = deg[b] < maxdeg ? deg[b] : maxdeg;
-    for (uint32_t i = 0; i < a; i++) {
-      const uint32_t x = tmp[b * maxdeg + i];
-      if (!contains(merged, c, x)) merged[c++] = x;
-    }
-    uint32_t k;
-    if (c > m_nn) {
-      for (uint32_t i = 0; i < c; i++) {
-        cid[i] = merged[i];
-        dist[i] = dist_avx(base + (uint64_t)merged[i] * d, base + b * d, d);
+  uint32_t* rows = (uint32_t*)malloc(sizeof(uint32_t) * n * m_nn);
+  uint32_t* rcnt = (uint32_t*)calloc(n, sizeof(uint32_t));
+#pragma omp parallel
+  {
+    float dist[256];
+    uint32_t cid[256];
+    uint32_t merged[128];
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t b = 0; b < (int64_t)n; b++) { /* :449-475 */
+      uint32_t c = 0;
+      for (uint32_t i = 0; i < pcnt[b]; i++) {
+        const uint32_t x = plist[(uint64_t)b * m_nn + i];
+        if (!contains(merged, c, x)) merged[c++] = x;
       }
-      sort_nb(dist, cid, c);
-      k = rng_prune(base, d, n, m_nn, dist, cid, c, (uint32_t)b, 1, res);
-    } else {
-      qsort(merged, c, sizeof(uint32_t), cmp_u32);
-      memcpy(res, merged, sizeof(uint32_t) * c);
-      k = c;
+      const uint32_t a = deg[b] < maxdeg ? deg[b] : maxdeg;
+      for (uint32_t i = 0; i < a; i++) {
+        const uint32_t x = tmp[(uint64_t)b * maxdeg + i];
+        if (!contains(merged, c, x)) merged[c++] = x;
+      }
+      uint32_t* out = rows + (uint64_t)b * m_nn;
+      if (c > m_nn) {
+        for (uint32_t i = 0; i < c; i++) {
+          cid[i] = merged[i];
+          dist[i] = dist_avx(base + (uint64_t)merged[i] * d, base + (uint64_t)b * d, d);
+        }
+        sort_nb(dist, cid, c);
+        rcnt[b] = rng_prune(base, d, n, m_nn, dist, cid, c, (uint32_t)b, 1, out);
+      } else {
+        qsort(merged, c, sizeof(uint32_t), cmp_u32);
+        memcpy(out, merged, sizeof(uint32_t) * c);
+        rcnt[b] = c;
+      }
     }
-    off[b] = o;
-    if (o + k > cap) {
-      ret = -1;
-      break;
-    }
-    memcpy(ids + o, res, sizeof(uint32_t) * k);
-    o += k;
   }
-  if (ret == 0) {
-    off[n] = o;
-    ret = (long long)o;
-  }
+  const long long ret = compact_rows(rows, rcnt, m_nn, n, off, ids, cap);
   free(match);
   free(claimed);
+  free(qlist);
+  free(qcnt);
   free(plist);
   free(pcnt);
   free(tmp);
   free(deg);
   free(full);
-  free(dist);
-  free(cid);
-  free(merged);
+  free(rows);
+  free(rcnt);
   return ret;
 }
 
@@ -248,43 +271,37 @@ long long pgo_fusion_nn(const float* base, uint64_t n, uint32_t d, uint32_t m_nn
                         uint32_t rounds, const uint64_t* sup_off, const uint32_t* sup_ids,
                         const uint64_t* sup_base, uint64_t* off, uint32_t* ids, uint64_t cap) {
   const uint32_t M = 2 * m_nn;
-  uint32_t ccap = 0;
+  uint64_t ccap = 0;
   for (uint64_t b = 0; b < n; b++) {
     uint64_t t = 0;
     for (uint32_t r = 0; r < rounds; r++)
       t += sup_off[r * (n + 1) + b + 1] - sup_off[r * (n + 1) + b];
-    if (t > ccap) ccap = (uint32_t)t;
+    if (t > ccap) ccap = t;
   }
-  float* dist = (float*)malloc(sizeof(float) * (ccap + 1));
-  uint32_t* cid = (uint32_t*)malloc(sizeof(uint32_t) * (ccap + 1));
-  uint32_t* res = (uint32_t*)malloc(sizeof(uint32_t) * (M + 1));
-  uint64_t o = 0;
-  long long ret = 0;
-  for (uint64_t b = 0; b < n; b++) {
-    uint32_t c = 0;
-    for (uint32_t r = 0; r < rounds; r++) {
-      const uint64_t* so = sup_off + r * (n + 1);
-      c = gather(sup_ids + sup_base[r] + so[b], so[b + 1] - so[b], n, (uint32_t)b, 1, cid, c);
+  uint32_t* rows = (uint32_t*)malloc(sizeof(uint32_t) * n * M);
+  uint32_t* rcnt = (uint32_t*)calloc(n, sizeof(uint32_t));
+#pragma omp parallel
+  {
+    float* dist = (float*)malloc(sizeof(float) * (ccap + 1));
+    uint32_t* cid = (uint32_t*)malloc(sizeof(uint32_t) * (ccap + 1));
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t b = 0; b < (int64_t)n; b++) {
+      uint32_t c = 0;
+      for (uint32_t r = 0; r < rounds; r++) {
+        const uint64_t* so = sup_off + r * (n + 1);
+        c = gather(sup_ids + sup_base[r] + so[b], so[b + 1] - so[b], n, (uint32_t)b, 1, cid, c);
+      }
+      for (uint32_t i = 0; i < c; i++)
+        dist[i] = dist_avx(base + (uint64_t)b * d, base + (uint64_t)cid[i] * d, d);
+      sort_nb(dist, cid, c);
+      rcnt[b] = rng_prune(base, d, n, M, dist, cid, c, (uint32_t)b, 1, rows + (uint64_t)b * M);
     }
-    for (uint32_t i = 0; i < c; i++)
-      dist[i] = dist_avx(base + b * d, base + (uint64_t)cid[i] * d, d);
-    sort_nb(dist, cid, c);
-    const uint32_t k = rng_prune(base, d, n, M, dist, cid, c, (uint32_t)b, 1, res);
-    off[b] = o;
-    if (o + k > cap) {
-      ret = -1;
-      break;
-    }
-    memcpy(ids + o, res, sizeof(uint32_t) * k);
-    o += k;
+    free(dist);
+    free(cid);
   }
-  if (ret == 0) {
-    off[n] = o;
-    ret = (long long)o;
-  }
-  free(dist);
-  free(cid);
-  free(res);
+  const long long ret = compact_rows(rows, rcnt, M, n, off, ids, cap);
+  free(rows);
+  free(rcnt);
   return ret;
 }
 
@@ -302,47 +319,45 @@ long long pgo_fusion_final(const float* base, uint64_t n, uint32_t d, uint32_t m
   for (uint64_t b = 0; b < n; b++)
     if (bip_off[b + 1] - bip_off[b] > bmax) bmax = bip_off[b + 1] - bip_off[b];
   const uint64_t ccap = bmax + m_link + m_supply + 1;
-  float* dist = (float*)malloc(sizeof(float) * ccap);
-  uint32_t* cid = (uint32_t*)malloc(sizeof(uint32_t) * ccap);
-  uint32_t* res = (uint32_t*)malloc(sizeof(uint32_t) * (m_final + 1));
-  uint32_t* fin = (uint32_t*)malloc(sizeof(uint32_t) * (ccap + m_final));
-  uint64_t o = 0;
-  long long ret = 0;
-  for (uint64_t b = 0; b < n; b++) {
-    uint32_t c = gather(bip_ids + bip_off[b], bip_off[b + 1] - bip_off[b], n, (uint32_t)b, 1, cid,
-                        0);
-    const uint32_t nbip = c;
-    memcpy(fin, cid, sizeof(uint32_t) * nbip);
-    c = gather(link + b * m_link, m_link, n, (uint32_t)b, 0, cid, c); /* self not skipped */
-    c = gather(supply + b * m_supply, m_supply, n, (uint32_t)b, 1, cid, c);
-    for (uint32_t i = 0; i < c; i++)
-      dist[i] = dist_avx(base + b * d, base + (uint64_t)cid[i] * d, d);
-    sort_nb(dist, cid, c);
-    const uint32_t k = rng_prune(base, d, n, m_final, dist, cid, c, (uint32_t)b, 1, res);
-    const uint64_t slots = m_final >= nbip ? (uint64_t)(m_final - nbip) : UINT64_MAX;
-    uint32_t nf = nbip, added = 0;
-    for (uint32_t i = 0; i < k; i++) {
-      if (added >= slots) break;
-      if (!contains(fin, nbip, res[i])) {
-        fin[nf++] = res[i];
-        added++;
+  const uint64_t stride = bmax + m_final;
+  uint32_t* rows = (uint32_t*)malloc(sizeof(uint32_t) * n * stride);
+  uint32_t* rcnt = (uint32_t*)calloc(n, sizeof(uint32_t));
+#pragma omp parallel
+  {
+    float* dist = (float*)malloc(sizeof(float) * ccap);
+    uint32_t* cid = (uint32_t*)malloc(sizeof(uint32_t) * ccap);
+    uint32_t* res = (uint32_t*)malloc(sizeof(uint32_t) * (m_final + 1));
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t bi = 0; bi < (int64_t)n; bi++) {
+      const uint64_t b = (uint64_t)bi;
+      uint32_t* fin = rows + b * stride;
+      uint32_t c = gather(bip_ids + bip_off[b], bip_off[b + 1] - bip_off[b], n, (uint32_t)b, 1,
+                          cid, 0);
+      const uint32_t nbip = c;
+      memcpy(fin, cid, sizeof(uint32_t) * nbip);
+      c = gather(link + b * m_link, m_link, n, (uint32_t)b, 0, cid, c); /* self not skipped */
+      c = gather(supply + b * m_supply, m_supply, n, (uint32_t)b, 1, cid, c);
+      for (uint32_t i = 0; i < c; i++)
+        dist[i] = dist_avx(base + b * d, base + (uint64_t)cid[i] * d, d);
+      sort_nb(dist, cid, c);
+      const uint32_t k = rng_prune(base, d, n, m_final, dist, cid, c, (uint32_t)b, 1, res);
+      const uint64_t slots = m_final >= nbip ? (uint64_t)(m_final - nbip) : UINT64_MAX;
+      uint32_t nf = nbip, added = 0;
+      for (uint32_t i = 0; i < k; i++) {
+        if (added >= slots) break;
+        if (!contains(fin, nbip, res[i])) {
+          fin[nf++] = res[i];
+          added++;
+        }
       }
+      rcnt[b] = nf;
     }
-    off[b] = o;
-    if (o + nf > cap) {
-      ret = -1;
-      break;
-    }
-    memcpy(ids + o, fin, sizeof(uint32_t) * nf);
-    o += nf;
+    free(dist);
+    free(cid);
+    free(res);
   }
-  if (ret == 0) {
-    off[n] = o;
-    ret = (long long)o;
-  }
-  free(dist);
-  free(cid);
-  free(res);
-  free(fin);
+  const long long ret = compact_rows(rows, rcnt, stride, n, off, ids, cap);
+  free(rows);
+  free(rcnt);
   return ret;
 }

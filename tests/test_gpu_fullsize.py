@@ -71,3 +71,29 @@ def test_full_size_screened_build_is_identical(workload):
     assert not bad.any(), f"{bad.sum()} rows differ between the plain and the screened build"
     assert stats[0].evals_total == stats[1].evals_total
     print("rescored", list(stats[1].rescored)[:2], "of", list(stats[1].evals_prune)[:2])
+
+
+def test_full_size_index_matches_oracle(workload):
+    """pg_build_index at 1M x 200 (the driver's whole index: GPU build, six MatchSup rounds,
+    FusionNN, FusionFinal) against the oracle's pipeline, list for list."""
+    import paragraph_gb300 as pg
+    base, gt = workload
+    params = pg.default_params(32, 64, screen=pg.SCREEN_BF16)
+    out = torch.full((N, 150), -1, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(N, dtype=torch.int32, device="cuda")
+    with pg.Handle(0) as h:
+        st = h.build_index(base, gt, out, cnt, params)
+    print(f"index 1M: {st.ms_total:.1f} ms (MatchSup {st.ms_match_sup:.1f}, FusionNN "
+          f"{st.ms_fusion_nn:.1f}, FusionFinal {st.ms_fusion_final:.1f})")
+    rows = out.cpu().numpy().view(np.uint32)
+    k = cnt.cpu().numpy().view(np.uint32).astype(np.int64)
+    base_np = base.cpu().numpy()
+    gt_np = gt.cpu().numpy().view(np.uint32)
+    g = oracle.build_graph(base_np, gt_np, degree=32, beam=64)
+    rounds = [oracle.match_sup(base_np, gt_np, r) for r in range(1, 7)]
+    fnn = oracle.fusion_nn(base_np, rounds)
+    off, ids = oracle.fusion_final(base_np, g["proj"], fnn, g["graph"])
+    ref_k = np.diff(off.astype(np.int64))
+    assert np.array_equal(k, ref_k), f"{(k != ref_k).sum()} row lengths differ"
+    mask = np.arange(rows.shape[1])[None, :] < k[:, None]
+    assert np.array_equal(rows[mask], ids), "index ids differ"
