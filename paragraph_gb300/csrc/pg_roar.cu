@@ -90,6 +90,31 @@ __device__ __forceinline__ const float* row_of(const float* base, uint32_t d, ui
   return base + static_cast<uint64_t>(id) * d;
 }
 
+// compare() computed by a group of 8 lanes: lane l of the group holds the accumulators of
+// elements 16c + l and 16c + 8 + l, so the 8+8 fold happens in the lane, the 4+4 fold and the two
+// horizontal adds by shuffles inside the group.  Every lane of the warp calls it (the shuffles
+// are warp-wide); the distance is valid in lane 0 of each group.  Same FP32 operations, in the
+// same order, as dist_avx; the group's loads are contiguous.
+__device__ __forceinline__ float dist_avx8(const float* __restrict__ a,
+                                           const float* __restrict__ b, uint32_t d, uint32_t l8) {
+  float lo = 0.0f, hi = 0.0f;
+  uint32_t i = 0;
+#pragma unroll 4
+  for (; i + 16 <= d; i += 16) {
+    lo = fmaf(__ldg(a + i + l8), __ldg(b + i + l8), lo);
+    hi = fmaf(__ldg(a + i + 8 + l8), __ldg(b + i + 8 + l8), hi);
+  }
+  float s8 = hi + lo;
+  if (d - i >= 8) {
+    s8 = fmaf(__ldg(a + i + l8), __ldg(b + i + l8), s8);
+    i += 8;
+  }
+  float s4 = __shfl_down_sync(kFull, s8, 4, 8) + s8;
+  if (d - i >= 4 && l8 < 4) s4 = fmaf(__ldg(a + i + l8), __ldg(b + i + l8), s4);
+  const float pr = s4 + __shfl_down_sync(kFull, s4, 1, 8);
+  return -(pr + __shfl_down_sync(kFull, pr, 2, 8));
+}
+
 // Replaces every repeat of an earlier id in cand[0..len) by tomb (first occurrences stay): a sort
 // of (id << 32 | position) keys puts the repeats of an id right after its first occurrence.
 template <int E>
@@ -118,15 +143,23 @@ __device__ void dedupe_first(uint32_t* cand, uint32_t len) {
 }
 
 // Distances from `node` to the non-tomb ids of cand[0..len), sorted by (distance, id) into
-// sid/sdist; returns their number.
+// sid/sdist; returns their number.  With `unique`, repeats of an id are dropped (they carry the
+// same distance, so they sit next to each other after the sort).
 template <int E>
 __device__ uint32_t sort_by_dist(const float* base, uint32_t d, uint32_t node,
-                                 const uint32_t* cand, uint32_t len, uint32_t* sid, float* sdist) {
-  const uint32_t lane = lane_id();
+                                 const uint32_t* cand, uint32_t len, uint32_t* sid, float* sdist,
+                                 bool unique) {
+  const uint32_t lane = lane_id(), g = lane >> 3, l8 = lane & 7u;
   const float* nrow = row_of(base, d, node);
+  for (uint32_t i0 = 0; i0 < len; i0 += 4) {  // four distances per pass
+    const uint32_t i = i0 + g;
+    const uint32_t x = i < len ? cand[i] : kTomb;
+    const float dist = dist_avx8(nrow, row_of(base, d, x != kTomb ? x : node), d, l8);
+    if (l8 == 0 && x != kTomb) sdist[i] = dist;
+  }
+  __syncwarp();
   uint64_t key[E];
   uint32_t val[E];
-  uint32_t cnt = 0;
 #pragma unroll
   for (int s = 0; s < E; s++) {
     const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
@@ -134,20 +167,27 @@ __device__ uint32_t sort_by_dist(const float* base, uint32_t d, uint32_t node,
     key[s] = ~0ull;
     val[s] = 0;
     if (x != kTomb) {
-      const float dist = dist_avx(nrow, row_of(base, d, x), d);
+      const float dist = sdist[i];
       key[s] = (static_cast<uint64_t>(order_key(dist)) << 32) | x;
       val[s] = __float_as_uint(dist);
     }
-    cnt += __popc(__ballot_sync(kFull, x != kTomb));
   }
+  __syncwarp();
   warp_sort_kv<E>(key, val);
+  uint32_t cnt = 0;
 #pragma unroll
   for (int s = 0; s < E; s++) {
-    const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
-    if (i < cnt) {
-      sid[i] = static_cast<uint32_t>(key[s]);
-      sdist[i] = __uint_as_float(val[s]);
+    const uint64_t up = __shfl_up_sync(kFull, key[s], 1);
+    const uint64_t wrap = s > 0 ? __shfl_sync(kFull, key[s > 0 ? s - 1 : 0], 31) : ~0ull;
+    const uint64_t prev = lane == 0 ? wrap : up;
+    const bool keep = key[s] != ~0ull && !(unique && prev == key[s]);
+    const unsigned m = __ballot_sync(kFull, keep);
+    if (keep) {
+      const uint32_t pos = cnt + __popc(m & ((1u << lane) - 1u));
+      sid[pos] = static_cast<uint32_t>(key[s]);
+      sdist[pos] = __uint_as_float(val[s]);
     }
+    cnt += __popc(m);
   }
   __syncwarp();
   return cnt;
@@ -156,13 +196,20 @@ __device__ uint32_t sort_by_dist(const float* base, uint32_t d, uint32_t node,
 template <int E>
 __device__ __forceinline__ uint32_t sort_by_dist_any(const float* base, uint32_t d, uint32_t node,
                                                      const uint32_t* cand, uint32_t len,
-                                                     uint32_t* sid, float* sdist) {
-  if (len <= 128) return sort_by_dist<4>(base, d, node, cand, len, sid, sdist);
-  return sort_by_dist<E>(base, d, node, cand, len, sid, sdist);
+                                                     uint32_t* sid, float* sdist,
+                                                     bool unique = false) {
+  if (len <= 32) return sort_by_dist<1>(base, d, node, cand, len, sid, sdist, unique);
+  if (len <= 64) return sort_by_dist<2>(base, d, node, cand, len, sid, sdist, unique);
+  if (len <= 128) return sort_by_dist<4>(base, d, node, cand, len, sid, sdist, unique);
+  return sort_by_dist<E>(base, d, node, cand, len, sid, sdist, unique);
 }
 
 __device__ __forceinline__ void dedupe_any(uint32_t* cand, uint32_t len) {
-  if (len <= 128)
+  if (len <= 32)
+    dedupe_first<1>(cand, len);
+  else if (len <= 64)
+    dedupe_first<2>(cand, len);
+  else if (len <= 128)
     dedupe_first<4>(cand, len);
   else
     dedupe_first<8>(cand, len);
@@ -186,20 +233,86 @@ __device__ uint32_t rng_prune_warp(const float* base, uint32_t d, uint64_t n, ui
   if (lane == 0) res[0] = sid[start];
   __syncwarp();
   uint32_t k = 1;
-  for (uint32_t j = start + 1; j < c && k < M; j++) {
-    const uint32_t p = sid[j];
-    const float pd = sdist[j];
+  const uint32_t g = lane >> 3, l8 = lane & 7u;
+  // The scan decides the candidates in order; four of them (a window, one per 8-lane group) are
+  // tested at once against the kept entries each has not been tested against yet.  The first
+  // candidate of the window that no kept entry occludes is kept; the ones before it are dropped,
+  // the ones after it stay in the window and are next tested against the new entry only.
+  uint32_t w[4], tested[4];
+  uint32_t wn = 0, next = start + 1;
+  while (k < M) {
+#pragma unroll
+    for (int e = 0; e < 4; e++)
+      if (static_cast<uint32_t>(e) == wn && next < c) {
+        w[e] = next++;
+        tested[e] = 0;
+        wn++;
+      }
+    if (wn == 0) break;
+    uint32_t my_w = w[0], my_t = tested[0], span = 0;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      if (static_cast<uint32_t>(e) < wn) span = max(span, k - tested[e]);
+      if (static_cast<uint32_t>(e) == g) {
+        my_w = w[e];
+        my_t = tested[e];
+      }
+    }
+    const bool mine = g < wn;
+    const uint32_t p = sid[mine ? my_w : w[0]];
+    const float pd = sdist[mine ? my_w : w[0]];
     const float* prow = row_of(base, d, p);
     bool occ = false;
-    for (uint32_t i = lane; i < k; i += 32) {
-      const uint32_t r = res[i];
-      occ |= r == p || dist_avx(prow, row_of(base, d, r), d) < pd;
+    for (uint32_t u = 0; u < span; u++) {
+      const uint32_t t = my_t + u;
+      const bool act = mine && t < k;
+      const uint32_t r = act ? res[t] : res[0];
+      const float dist = dist_avx8(prow, row_of(base, d, r), d, l8);
+      occ |= act && l8 == 0 && (r == p || dist < pd);
     }
-    if (__ballot_sync(kFull, occ) == 0 && p != target) {
-      if (lane == 0) res[k] = p;
-      k++;
-      __syncwarp();
+    const unsigned bits = __ballot_sync(kFull, occ);
+    const uint32_t k_old = k;
+    int kept = -1;
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      if (kept < 0 && static_cast<uint32_t>(e) < wn && ((bits >> (8 * e)) & 1u) == 0) {
+        const uint32_t x = sid[w[e]];
+        if (x != target) {  // not occluded: kept (the node itself never is, :133-137)
+          if (lane == 0) res[k] = x;
+          k++;
+          kept = e;
+        }
+      }
     }
+    __syncwarp();
+    // the window keeps the entries after the kept one that nothing occludes yet, tested against
+    // res[0 .. k_old); the occluded ones are decided
+    uint32_t nw = 0;
+    uint32_t w2[4], t2[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      w2[e] = 0;
+      t2[e] = 0;
+    }
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      if (kept >= 0 && e > kept && static_cast<uint32_t>(e) < wn &&
+          ((bits >> (8 * e)) & 1u) == 0) {
+#pragma unroll
+        for (int f = 0; f < 4; f++)
+          if (static_cast<uint32_t>(f) == nw) {
+            w2[f] = w[e];
+            t2[f] = k_old;
+          }
+        nw++;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      w[e] = w2[e];
+      tested[e] = t2[e];
+    }
+    wn = nw;
   }
   if (!strict) {  // :168-176
     for (uint32_t i = 1; i < c && k < M; i++) {
@@ -213,6 +326,25 @@ __device__ uint32_t rng_prune_warp(const float* base, uint32_t d, uint64_t n, ui
   }
   __syncwarp();
   return k;
+}
+
+// The u non-tomb ids of cand[0..len) in ascending order into out.
+template <int E>
+__device__ __forceinline__ void write_ascending(const uint32_t* cand, uint32_t len, uint32_t u,
+                                                uint32_t* out) {
+  const uint32_t lane = lane_id();
+  uint32_t v[E];
+#pragma unroll
+  for (int s = 0; s < E; s++) {
+    const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
+    v[s] = i < len ? cand[i] : kTomb;
+  }
+  warp_sort_u32<E>(v);
+#pragma unroll
+  for (int s = 0; s < E; s++) {
+    const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
+    if (i < u) out[i] = v[s];
+  }
 }
 
 __device__ __forceinline__ RoarSmem* warp_smem(RoarSmem* all) {
@@ -268,8 +400,8 @@ __global__ void __launch_bounds__(kRoarWarps * 32) k_sup_prune(SupArgs a) {
       sm->cand[i] = (i < stop && x != nn) ? x : kTomb;
     }
     __syncwarp();
-    dedupe_any(sm->cand, a.gt_k);
-    const uint32_t c = sort_by_dist_any<8>(a.base, a.d, nn, sm->cand, a.gt_k, sm->sid, sm->sdist);
+    const uint32_t c =
+        sort_by_dist_any<8>(a.base, a.d, nn, sm->cand, a.gt_k, sm->sid, sm->sdist, true);
     const uint32_t k =
         rng_prune_warp(a.base, a.d, a.n, a.m_nn, sm->sid, sm->sdist, c, nn, false, sm->res);
     for (uint32_t i = lane; i < k; i += 32) {
@@ -299,6 +431,10 @@ __global__ void __launch_bounds__(kRoarWarps * 32) k_sup_merge(SupArgs a) {
       sm->cand[k1 + i] = a.gt[src * a.gt_k + a.topn];
     }
     const uint32_t len = k1 + r;
+    if (len == 0) {
+      if (lane == 0) a.cnt[b] = 0;
+      continue;
+    }
     __syncwarp();
     dedupe_any(sm->cand, len);
     uint32_t u = 0;
@@ -312,19 +448,13 @@ __global__ void __launch_bounds__(kRoarWarps * 32) k_sup_merge(SupArgs a) {
                                         static_cast<uint32_t>(b), true, sm->res);
       for (uint32_t i = lane; i < k; i += 32) out[i] = sm->res[i];
       if (lane == 0) a.cnt[b] = k;
-    } else {  // at most M_nn <= 128 ids: ascending
-      uint32_t v[4];
-#pragma unroll
-      for (int s = 0; s < 4; s++) {
-        const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
-        v[s] = i < len ? sm->cand[i] : kTomb;
-      }
-      warp_sort_u32<4>(v);
-#pragma unroll
-      for (int s = 0; s < 4; s++) {
-        const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
-        if (i < u) out[i] = v[s];
-      }
+    } else {  // at most M_nn ids: ascending
+      if (len <= 32)
+        write_ascending<1>(sm->cand, len, u, out);
+      else if (len <= 64)
+        write_ascending<2>(sm->cand, len, u, out);
+      else
+        write_ascending<4>(sm->cand, len, u, out);
       if (lane == 0) a.cnt[b] = u;
     }
     __syncwarp();
@@ -350,9 +480,8 @@ __global__ void __launch_bounds__(kRoarWarps * 32) k_fusion_nn(FusionArgs a) {
       len += k;
     }
     __syncwarp();
-    dedupe_any(sm->cand, len);
     const uint32_t c = sort_by_dist_any<8>(a.base, a.d, static_cast<uint32_t>(b), sm->cand, len,
-                                           sm->sid, sm->sdist);
+                                           sm->sid, sm->sdist, true);
     const uint32_t k = rng_prune_warp(a.base, a.d, a.n, a.m_out, sm->sid, sm->sdist, c,
                                       static_cast<uint32_t>(b), true, sm->res);
     for (uint32_t i = lane; i < k; i += 32) a.out[b * a.out_stride + i] = sm->res[i];
