@@ -138,6 +138,117 @@ __device__ __forceinline__ bool occluded(const float* __restrict__ base, uint64_
   return false;
 }
 
+// The occlusion scan of fusion_prune_reverse_kernel_v0 (Gbuilder.cuh:1150-1199) and
+// fusion_merge_sort_prune_kernel over the sorted candidates ids_s/dist_s[j0 .. c): in order, a
+// candidate is kept when no kept entry lies closer to it than the node does (exact FP32 chain),
+// until `limit` are kept.  Many candidates are tested at once: the lanes take (candidate, kept
+// entry) pairs of a window of consecutive undecided candidates, each candidate against the kept
+// entries it has not been tested against yet.  Candidates are decided from the front of the
+// window -- occluded ones dropped, the first unoccluded one kept, which sends the later ones back
+// for one more test against it.  Kept entries and the evaluation count (tests up to the first
+// occluder, as occluded() counts them) equal the one-candidate-at-a-time scan.  kept_s[0 .. K)
+// on entry; returns where that scan stops: the candidate that filled the list, the first tomb
+// (stop_at_tomb), or c.  Ids >= n count as occluded without a test.  win: 96 words per warp.
+constexpr uint32_t kWinNone = 0xFFFFFFFFu, kWinInvalid = 0xFFFFFFFEu;
+
+__device__ uint32_t scan_kept(const float* __restrict__ base, uint64_t n, uint32_t d,
+                              const uint32_t* ids_s, const float* dist_s, uint32_t j0, uint32_t c,
+                              uint32_t* kept_s, uint32_t& K, uint32_t limit, bool stop_at_tomb,
+                              uint32_t* win, uint64_t* checks) {
+  const uint32_t lane = lane_id();
+  uint32_t* wj = win;        // candidate position
+  uint32_t* wt = win + 32;   // kept entries tested so far without an occluder
+  uint32_t* wo = win + 64;   // first occluder, kWinNone, or kWinInvalid
+  uint32_t next = j0, wn = 0;
+  for (;;) {
+    while (wn < 32 && next < c) {
+      const uint32_t x = ids_s[next];
+      if (stop_at_tomb && (x == kTomb || x == kMaskedTomb)) break;
+      if (lane == 0) {
+        wj[wn] = next;
+        wt[wn] = 0;
+        wo[wn] = x >= n ? kWinInvalid : kWinNone;
+      }
+      wn++;
+      next++;
+    }
+    __syncwarp();
+    if (wn == 0) return next;
+    // lanes -> (candidate, kept entry) pairs, front of the window first
+    uint32_t my_w = kWinNone, my_t = 0, acc = 0;
+    for (uint32_t w = 0; w < wn && acc < 32; w++) {
+      if (wo[w] != kWinNone) continue;
+      const uint32_t need = K - wt[w];
+      if (lane >= acc && lane < acc + need) {
+        my_w = w;
+        my_t = wt[w] + (lane - acc);
+      }
+      acc += need;
+    }
+    bool o = false;
+    if (my_w != kWinNone) {
+      const uint32_t pos = wj[my_w];
+      o = dist_seq(base + static_cast<uint64_t>(ids_s[pos]) * d,
+                   base + static_cast<uint64_t>(kept_s[my_t]) * d, d) < dist_s[pos];
+    }
+    const unsigned mask = __ballot_sync(kFull, o);
+    acc = 0;
+    for (uint32_t w = 0; w < wn && acc < 32; w++) {
+      if (wo[w] != kWinNone) continue;
+      const uint32_t take = min(K - wt[w], 32u - acc);
+      const unsigned range = (take >= 32 ? kFull : ((1u << take) - 1u)) << acc;
+      const unsigned m = mask & range;
+      if (lane == 0) {
+        if (m)
+          wo[w] = wt[w] + (static_cast<uint32_t>(__ffs(static_cast<int>(m)) - 1) - acc);
+        else
+          wt[w] += take;
+      }
+      acc += take;
+    }
+    __syncwarp();
+    uint32_t dec = 0;
+    for (uint32_t w = 0; w < wn; w++) {
+      const uint32_t oc = wo[w];
+      if (oc == kWinInvalid) {
+        dec++;
+        continue;
+      }
+      if (oc != kWinNone) {
+        *checks += oc + 1;
+        dec++;
+        continue;
+      }
+      if (wt[w] != K) break;  // undecided: later candidates wait for it
+      *checks += K;
+      if (lane == 0) kept_s[K] = ids_s[wj[w]];
+      K++;
+      dec++;
+      if (K == limit) {
+        __syncwarp();
+        return wj[w];
+      }
+    }
+    __syncwarp();
+    if (dec) {  // drop the decided front of the window
+      uint32_t a = 0, b = 0, e = 0;
+      if (lane + dec < wn) {
+        a = wj[lane + dec];
+        b = wt[lane + dec];
+        e = wo[lane + dec];
+      }
+      __syncwarp();
+      if (lane + dec < wn) {
+        wj[lane] = a;
+        wt[lane] = b;
+        wo[lane] = e;
+      }
+      wn -= dec;
+      __syncwarp();
+    }
+  }
+}
+
 __device__ __forceinline__ float key_dist(uint64_t key) {
   const uint32_t o = static_cast<uint32_t>(key >> 32);
   const uint32_t u = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
@@ -153,9 +264,10 @@ __global__ void __launch_bounds__(256) k_prune_reverse(PruneArgs a) {
   extern __shared__ uint32_t smem_u32[];
   const uint32_t lane = lane_id();
   const uint32_t warp = threadIdx.x >> 5;
-  uint32_t* ids_s = smem_u32 + warp * (3 * C_MAX);
+  uint32_t* ids_s = smem_u32 + warp * (3 * C_MAX + 96);
   float* dist_s = reinterpret_cast<float*>(ids_s + C_MAX);
   uint32_t* kept_s = ids_s + 2 * C_MAX;
+  uint32_t* win_s = ids_s + 3 * C_MAX;
   const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (blockDim.x >> 5);
   uint64_t ev = 0;
   for (uint64_t b = blockIdx.x * static_cast<uint64_t>(blockDim.x >> 5) + warp; b < a.n;
@@ -232,19 +344,12 @@ __global__ void __launch_bounds__(256) k_prune_reverse(PruneArgs a) {
     }
     if (lane == 0) kept_s[0] = first;
     __syncwarp();
-    uint32_t k = 0;
-    uint32_t j = 1;
     uint64_t checks = 0;
-    for (; j < a.c; j++) {
-      const uint32_t p = ids_s[j];
-      if (p == kTomb || p == kMaskedTomb) break;
-      if (!occluded(a.base, a.n, a.d, p, dist_s[j], kept_s, k, &checks)) {
-        k++;
-        if (lane == 0) kept_s[k] = p;
-        __syncwarp();
-        if (k == a.p - 1) break;
-      }
-    }
+    uint32_t kc = 1;
+    uint32_t j = a.p > 1 ? scan_kept(a.base, a.n, a.d, ids_s, dist_s, 1, a.c, kept_s, kc, a.p, true,
+                                     win_s, &checks)
+                         : 1;
+    uint32_t k = kc - 1;
     if (!a.strict && k < a.p - 1) {  // non-strict fill (Gbuilder.cuh:1201-1239)
       for (uint32_t j2 = j; j2 < a.c && k < a.p - 1; j2++) {
         const uint32_t x = ids_s[j2];
@@ -436,10 +541,11 @@ __global__ void __launch_bounds__(256) k_merge_prune(MergeArgs a) {
   extern __shared__ uint32_t smem_u32[];
   const uint32_t lane = lane_id();
   const uint32_t warp = threadIdx.x >> 5;
-  uint32_t* ids_s = smem_u32 + warp * (3 * C_MAX + C_MAX / 4);
+  uint32_t* ids_s = smem_u32 + warp * (3 * C_MAX + C_MAX / 4 + 96);
   float* dist_s = reinterpret_cast<float*>(ids_s + C_MAX);
   uint32_t* out_s = ids_s + 2 * C_MAX;
   uint8_t* added_s = reinterpret_cast<uint8_t*>(ids_s + 3 * C_MAX);
+  uint32_t* win_s = ids_s + 3 * C_MAX + C_MAX / 4;
   const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (blockDim.x >> 5);
   uint64_t ev = 0;
   for (uint64_t b = blockIdx.x * static_cast<uint64_t>(blockDim.x >> 5) + warp; b < a.n;
@@ -490,17 +596,11 @@ __global__ void __launch_bounds__(256) k_merge_prune(MergeArgs a) {
     __syncwarp();
     if (lane == 0) out_s[0] = ids_s[0];
     __syncwarp();
-    uint32_t k = 0;
     uint64_t checks = 0;
-    for (uint32_t j = 1; j < nn; j++) {
-      const uint32_t x = ids_s[j];
-      if (!occluded(a.base, a.n, a.d, x, dist_s[j], out_s, k, &checks)) {
-        k++;
-        if (lane == 0) out_s[k] = x;
-        __syncwarp();
-        if (k == a.degree - 1) break;
-      }
-    }
+    uint32_t kc = 1;
+    if (a.degree > 1)
+      scan_kept(a.base, a.n, a.d, ids_s, dist_s, 1, nn, out_s, kc, a.degree, false, win_s, &checks);
+    uint32_t k = kc - 1;
     if (!a.strict && k < a.degree - 1) {
       for (uint32_t i = lane; i < nn; i += 32) added_s[i] = 0;
       __syncwarp();
@@ -585,7 +685,7 @@ cudaError_t launch_validate_ids(const uint32_t* ids, uint64_t count, uint64_t n,
 template <int E, bool P1>
 static cudaError_t launch_prune_e(const PruneArgs& a, int num_sms, cudaStream_t st) {
   const int threads = 256;
-  const size_t smem = (threads / 32) * 3 * 32 * E * sizeof(uint32_t);
+  const size_t smem = (threads / 32) * (3 * 32 * E + 96) * sizeof(uint32_t);
   k_prune_reverse<E, P1><<<grid_for(a.n, threads / 32, num_sms, 8), threads, smem, st>>>(a);
   return cudaGetLastError();
 }
@@ -625,7 +725,7 @@ cudaError_t launch_reverse_lists(const uint32_t* offs, const uint32_t* edges, ui
 template <int E>
 static cudaError_t launch_merge_e(const MergeArgs& a, int num_sms, cudaStream_t st) {
   const int threads = 256;
-  const size_t smem = (threads / 32) * (3 * 32 * E + 8 * E) * sizeof(uint32_t);
+  const size_t smem = (threads / 32) * (3 * 32 * E + 8 * E + 96) * sizeof(uint32_t);
   k_merge_prune<E><<<grid_for(a.n, threads / 32, num_sms, 8), threads, smem, st>>>(a);
   return cudaGetLastError();
 }

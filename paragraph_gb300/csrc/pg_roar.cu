@@ -115,6 +115,41 @@ __device__ __forceinline__ float dist_avx8(const float* __restrict__ a,
   return -(pr + __shfl_down_sync(kFull, pr, 2, 8));
 }
 
+// Two dist_avx8 at once (a against b0 and against b1), for twice the loads in flight.
+__device__ __forceinline__ void dist_avx8x2(const float* __restrict__ a,
+                                            const float* __restrict__ b0,
+                                            const float* __restrict__ b1, uint32_t d, uint32_t l8,
+                                            float& r0, float& r1) {
+  float lo0 = 0.0f, hi0 = 0.0f, lo1 = 0.0f, hi1 = 0.0f;
+  uint32_t i = 0;
+#pragma unroll 2
+  for (; i + 16 <= d; i += 16) {
+    const float x0 = __ldg(a + i + l8), x1 = __ldg(a + i + 8 + l8);
+    lo0 = fmaf(x0, __ldg(b0 + i + l8), lo0);
+    hi0 = fmaf(x1, __ldg(b0 + i + 8 + l8), hi0);
+    lo1 = fmaf(x0, __ldg(b1 + i + l8), lo1);
+    hi1 = fmaf(x1, __ldg(b1 + i + 8 + l8), hi1);
+  }
+  float s0 = hi0 + lo0, s1 = hi1 + lo1;
+  if (d - i >= 8) {
+    const float x = __ldg(a + i + l8);
+    s0 = fmaf(x, __ldg(b0 + i + l8), s0);
+    s1 = fmaf(x, __ldg(b1 + i + l8), s1);
+    i += 8;
+  }
+  float t0 = __shfl_down_sync(kFull, s0, 4, 8) + s0;
+  float t1 = __shfl_down_sync(kFull, s1, 4, 8) + s1;
+  if (d - i >= 4 && l8 < 4) {
+    const float x = __ldg(a + i + l8);
+    t0 = fmaf(x, __ldg(b0 + i + l8), t0);
+    t1 = fmaf(x, __ldg(b1 + i + l8), t1);
+  }
+  const float p0 = t0 + __shfl_down_sync(kFull, t0, 1, 8);
+  const float p1 = t1 + __shfl_down_sync(kFull, t1, 1, 8);
+  r0 = -(p0 + __shfl_down_sync(kFull, p0, 2, 8));
+  r1 = -(p1 + __shfl_down_sync(kFull, p1, 2, 8));
+}
+
 // Replaces every repeat of an earlier id in cand[0..len) by tomb (first occurrences stay): a sort
 // of (id << 32 | position) keys puts the repeats of an id right after its first occurrence.
 template <int E>
@@ -151,11 +186,15 @@ __device__ uint32_t sort_by_dist(const float* base, uint32_t d, uint32_t node,
                                  bool unique) {
   const uint32_t lane = lane_id(), g = lane >> 3, l8 = lane & 7u;
   const float* nrow = row_of(base, d, node);
-  for (uint32_t i0 = 0; i0 < len; i0 += 4) {  // four distances per pass
-    const uint32_t i = i0 + g;
+  for (uint32_t i0 = 0; i0 < len; i0 += 8) {  // eight distances per pass, two per 8-lane group
+    const uint32_t i = i0 + g, j = i0 + 4 + g;
     const uint32_t x = i < len ? cand[i] : kTomb;
-    const float dist = dist_avx8(nrow, row_of(base, d, x != kTomb ? x : node), d, l8);
-    if (l8 == 0 && x != kTomb) sdist[i] = dist;
+    const uint32_t y = j < len ? cand[j] : kTomb;
+    float dx, dy;
+    dist_avx8x2(nrow, row_of(base, d, x != kTomb ? x : node), row_of(base, d, y != kTomb ? y : node),
+                d, l8, dx, dy);
+    if (l8 == 0 && x != kTomb) sdist[i] = dx;
+    if (l8 == 0 && y != kTomb) sdist[j] = dy;
   }
   __syncwarp();
   uint64_t key[E];
