@@ -16,7 +16,8 @@ make_golden.py (same base and ground truth) this records:
               of the case's projection and M=32 link graph, CSR
   cmp         compare() on 2000 seeded pairs                          :31-80
 
-and ref_cpu_ffwrap_1000x200.npz: FusionFinal alone on crafted bipartite lists (see run_wrap).
+and ref_cpu_ffwrap_1000x200.npz: FusionFinal alone on crafted bipartite lists (see run_wrap);
+ref_cpu_compare_tails.npz: compare() at dimensions that reach its 8- and 4-wide tails.
 """
 from __future__ import annotations
 
@@ -130,6 +131,22 @@ def run_wrap(L):
     print("wrote", path)
 
 
+def run_compare_tails(L):
+    """compare() at dimensions that reach its 8-wide and 4-wide tails (:44-64): D = 4, 12, 20, 36,
+    52, 204 on seeded vectors."""
+    rng = np.random.default_rng(23)
+    out = {}
+    for d in (4, 12, 20, 36, 52, 204):
+        a = rng.standard_normal((300, d)).astype(np.float32) * 3
+        b = rng.standard_normal((300, d)).astype(np.float32)
+        out[f"a{d}"], out[f"b{d}"] = a, b
+        out[f"v{d}"] = np.array([L.ref_cpu_compare(a[i].ctypes.data, b[i].ctypes.data, d)
+                                 for i in range(300)], dtype=np.float32)
+    path = os.path.join(HERE, "ref_cpu_compare_tails.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path)
+
+
 def main():
     if not os.path.exists(LIB):
         sys.exit(f"{LIB} is missing: run oracle/build_ref_cpu.sh first")
@@ -137,6 +154,7 @@ def main():
     for name in ("mix", "edge"):
         run_case(L, name)
     run_wrap(L)
+    run_compare_tails(L)
 
 
 if __name__ == "__main__":

@@ -104,9 +104,9 @@ def test_fusion_final_equals_reference(pg, golden_dir, case):
         assert np.array_equal(got[i], ref[i]), f"FusionFinal node {i}"
 
 
-def test_build_index_equals_oracle_pipeline(pg):
+@pytest.mark.parametrize("n,d", [(3000, 64), (2500, 44)])  # 44 = 2*16 + 8 + 4: both tails
+def test_build_index_equals_oracle_pipeline(pg, n, d):
     from paragraph_gb300 import datagen
-    n, d = 3000, 64
     base, gt = datagen.make_dataset(n, d, seed=808)
     params = pg.default_params(32, 64)
     out = u32(n, 2 * M_NN + 70)

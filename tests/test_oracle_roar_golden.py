@@ -70,3 +70,12 @@ def test_fusion_final_long_bipartite_lists(golden_dir):
                                    f["link32_graph"])
     assert np.array_equal(off, w["ff_off"]) and np.array_equal(ids, w["ff_ids"])
     assert np.diff(w["ff_off"].astype(np.int64)).max() > 70
+
+
+def test_compare_tails_bit_exact(golden_dir):
+    """compare()'s 8- and 4-wide tails (tests/test_t2iend.cu:44-64) at D = 4 .. 204."""
+    t = dict(np.load(os.path.join(golden_dir, "ref_cpu_compare_tails.npz")))
+    for d in (4, 12, 20, 36, 52, 204):
+        got = np.array([oracle.dist_avx(a, b) for a, b in zip(t[f"a{d}"], t[f"b{d}"])],
+                       np.float32)
+        assert np.array_equal(got.view(np.uint32), t[f"v{d}"].view(np.uint32)), f"D={d}"
