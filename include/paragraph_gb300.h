@@ -186,6 +186,16 @@ int pg_build_index(pg_handle h, const pg_params* p, const float* d_base, uint64_
                    uint32_t m_final, uint32_t out_stride, uint32_t* d_out, uint32_t* d_cnt,
                    pg_stats* st);
 
+/* ---- ground truth (the reference reads it from files made outside its build, README.md:25-31)
+ * pg_ground_truth: for each of nq queries (nq x d, device) the k ids of the base rows (n x d)
+ * with the largest inner product, best first -- exact: ranked by FP64 inner products, ties to the
+ * lower id.  Candidates are screened on tensor cores (FP16 operands, FP32 accumulation) with a
+ * rigorous error margin, and every candidate inside the margin is re-scored in FP64.  k <= 256;
+ * rows past n are tomb.  PG_EUNSUPPORTED when a value exceeds the FP16 range (|x| > 65000) or the
+ * margin holds more candidates than the selection can keep (1024 per query). */
+int pg_ground_truth(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
+                    const float* d_queries, uint64_t nq, uint32_t k, uint32_t* d_out);
+
 /* ---- autotuning (no counterpart in the reference: its launch shapes, beam width and hash
  * capacity are compile-time constants, tests/test_t2iend.cu:671-727) --------------------------
  * pg_set_tuning / pg_get_tuning: the tuning later builds on this handle use.

@@ -84,6 +84,9 @@ def lib():
                                        ctypes.c_uint32, ctypes.c_uint32, _u32p, _u64p, _u32p,
                                        _u32p, _u64p, _u32p, ctypes.c_uint64]
         L.pgo_fusion_final.restype = ctypes.c_longlong
+        L.pgo_ground_truth.argtypes = [_f32p, ctypes.c_uint64, ctypes.c_uint32, _f32p,
+                                       ctypes.c_uint64, ctypes.c_uint32, _u32p]
+        L.pgo_ground_truth.restype = None
         _LIB = L
     return _LIB
 
@@ -359,3 +362,13 @@ def fusion_final(base, supply, bip, link, m_final: int = 70):
                                _p(link, _u32p), _p(off, _u64p), _p(ids, _u32p), ids.shape[0])
     assert k >= 0
     return off, ids[:k].copy()
+
+
+def ground_truth(base, queries, k: int = 128) -> np.ndarray:
+    """Exact inner-product top-k: FP64 sequential dot products, ties to the lower id."""
+    base = _f32(base)
+    queries = _f32(queries)
+    out = np.empty((queries.shape[0], k), dtype=np.uint32)
+    lib().pgo_ground_truth(_p(base, _f32p), base.shape[0], base.shape[1], _p(queries, _f32p),
+                           queries.shape[0], k, _p(out, _u32p))
+    return out

@@ -361,3 +361,44 @@ long long pgo_fusion_final(const float* base, uint64_t n, uint32_t d, uint32_t m
   free(rcnt);
   return ret;
 }
+
+/* ---------------------------------------------------------------- ground truth */
+
+static int gt_better(double a, uint32_t ia, double b, uint32_t ib) {
+  return a > b || (a == b && ia < ib);
+}
+
+/* Exact inner-product top-k (the definition pg_ground_truth implements): for each query the k
+ * base ids with the largest FP64 inner product (sequential FMA over d), ties to the lower id,
+ * best first; tomb past n. */
+void pgo_ground_truth(const float* base, uint64_t n, uint32_t d, const float* queries,
+                      uint64_t nq, uint32_t k, uint32_t* out) {
+#pragma omp parallel
+  {
+    double* hs = (double*)malloc(sizeof(double) * (k + 1));
+    uint32_t* hi = (uint32_t*)malloc(sizeof(uint32_t) * (k + 1));
+#pragma omp for schedule(dynamic, 4)
+    for (int64_t qi = 0; qi < (int64_t)nq; qi++) {
+      const float* q = queries + (uint64_t)qi * d;
+      uint32_t cnt = 0; /* sorted best-first list of the best k so far */
+      for (uint64_t x = 0; x < n; x++) {
+        const float* r = base + x * d;
+        double s = 0.0;
+        for (uint32_t j = 0; j < d; j++) s = fma((double)q[j], (double)r[j], s);
+        if (cnt == k && !gt_better(s, (uint32_t)x, hs[k - 1], hi[k - 1])) continue;
+        uint32_t pos = cnt < k ? cnt : k - 1;
+        while (pos > 0 && gt_better(s, (uint32_t)x, hs[pos - 1], hi[pos - 1])) {
+          hs[pos] = hs[pos - 1];
+          hi[pos] = hi[pos - 1];
+          pos--;
+        }
+        hs[pos] = s;
+        hi[pos] = (uint32_t)x;
+        if (cnt < k) cnt++;
+      }
+      for (uint32_t i = 0; i < k; i++) out[(uint64_t)qi * k + i] = i < cnt ? hi[i] : TOMB;
+    }
+    free(hs);
+    free(hi);
+  }
+}

@@ -121,6 +121,7 @@ SIGNATURES = {
                                        _U32, _U32, _U32, _VP, _VP]),
     "pg_build_index": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _U64, _U32, _VP, _U64,
                                       _U32, _U32, _U32, _U32, _VP, _VP, ctypes.POINTER(Stats)]),
+    "pg_ground_truth": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _U64, _U32, _VP]),
     "pg_set_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
     "pg_get_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
     "pg_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _U32, _VP, _VP, _VP, _U32,
@@ -336,6 +337,12 @@ class Handle:
                                     gt.shape[0], match_rounds, m_nn, m_final, out.shape[1],
                                     _ptr(out), _ptr(cnt), ctypes.byref(st)))
         return st
+
+    def ground_truth(self, base, queries, out):
+        """pg_ground_truth: exact inner-product top-k (k = out.shape[1]) of every query."""
+        n, d = base.shape
+        _check(lib().pg_ground_truth(self._h, _ptr(base), n, d, _ptr(queries), queries.shape[0],
+                                     out.shape[1], _ptr(out)))
 
     def set_tuning(self, tuning: Tuning):
         _check(lib().pg_set_tuning(self._h, ctypes.byref(tuning)))

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libparagraph_gb300.so")
 SOURCES = ["pg_api.cu", "pg_graph.cu", "pg_search.cu", "pg_screen.cu", "pg_noalloc.cu",
-           "pg_roar.cu"]
+           "pg_roar.cu", "pg_gt.cu"]
 HEADERS = ["pg_device.cuh", "pg_kernels.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
@@ -63,7 +63,9 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cudalib = os.path.join(os.path.dirname(os.path.dirname(cc)), "lib64")
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcublas", "-lcudart", "-Xlinker", "-rpath",
+           "-Xlinker", cudalib]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -143,6 +143,43 @@ __device__ __forceinline__ void warp_sort_u32(uint32_t (&key)[E]) {
   }
 }
 
+// Sort 32*E uint64 keys ascending (same layout as warp_sort_kv).
+template <int E>
+__device__ __forceinline__ void warp_sort_u64(uint64_t (&key)[E]) {
+  const uint32_t lane = threadIdx.x & 31u;
+  constexpr uint32_t n = 32u * E;
+#pragma unroll
+  for (uint32_t k = 2; k <= n; k <<= 1) {
+#pragma unroll
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+        const uint32_t js = j >> 5;
+#pragma unroll
+        for (int s = 0; s < E; s++) {
+          const int s2 = s ^ static_cast<int>(js);
+          if (s2 > s) {
+            const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
+            const bool asc = (i & k) == 0;
+            const uint64_t a = key[s], b = key[s2];
+            const bool sw = asc ? (a > b) : (a < b);
+            key[s] = sw ? b : a;
+            key[s2] = sw ? a : b;
+          }
+        }
+      } else {
+        const bool lower = (lane & j) == 0;
+#pragma unroll
+        for (int s = 0; s < E; s++) {
+          const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
+          const bool asc = (i & k) == 0;
+          const uint64_t o = __shfl_xor_sync(kFull, key[s], j);
+          key[s] = (lower == asc) ? (o < key[s] ? o : key[s]) : (o > key[s] ? o : key[s]);
+        }
+      }
+    }
+  }
+}
+
 // Merge stages only (the input is bitonic): sorts ascending in log2(32E) steps.
 template <int E>
 __device__ __forceinline__ void warp_bitonic_merge_u32(uint32_t (&key)[E]) {

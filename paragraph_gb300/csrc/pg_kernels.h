@@ -3,6 +3,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+struct cublasContext;  // cublasHandle_t
+
 namespace pg {
 
 struct PruneArgs {
@@ -130,6 +132,15 @@ cudaError_t launch_sup_merge(const SupArgs& a, int num_sms, cudaStream_t st);
 cudaError_t launch_fusion_nn(const FusionArgs& a, int num_sms, cudaStream_t st);
 cudaError_t launch_fusion_final(const FusionArgs& a, int num_sms, cudaStream_t st);
 
+// Exact inner-product top-k ground truth (pg_gt.cu).  Returns 0, a negative cudaError_t, or a
+// positive code for a cuBLAS failure; device-side overflow sets kErrCapacity in *status.
+uint32_t gt_max_k();
+size_t gt_chunk_rows(uint64_t n, uint64_t nq);
+size_t gt_workspace_bytes(uint64_t n, uint64_t nq, uint32_t d, uint32_t segs);
+int ground_truth(cublasContext* blas, const float* base, uint64_t n, uint32_t d,
+                 const float* queries, uint64_t nq, uint32_t k, uint32_t* out, char* ws,
+                 uint32_t* status, int num_sms, cudaStream_t st, float* diag = nullptr);
+
 cudaError_t launch_match_winner(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint64_t n,
                                 uint32_t* winner, uint32_t* status, int num_sms, cudaStream_t st,
                                 const uint64_t* seg_off = nullptr,
@@ -141,7 +152,7 @@ cudaError_t launch_match_rows(const uint32_t* gt, uint32_t gt_k, uint64_t n,
                               const uint32_t* winner, uint32_t* out, int num_sms,
                               cudaStream_t st);
 cudaError_t launch_validate_ids(const uint32_t* ids, uint64_t count, uint64_t n,
-                                uint32_t* status, int num_sms, cudaStream_t st);
+                                uint32_t* status, int num_sms, cudaStream_t st, float* diag = nullptr);
 cudaError_t launch_prune_reverse(const PruneArgs& a, bool phase1, int num_sms, cudaStream_t st);
 // Reverse edges as CSR over n destinations: offs = exclusive scan of indeg, edges grouped by
 // destination holding the source row index.  `rows` pruned rows are scanned (0 = n).
