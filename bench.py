@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--no-index", action="store_true",
                     help="skip timing the whole index (pg_build_index: build + RoarGraph path + "
                          "FusionFinal)")
+    ap.add_argument("--no-gt", action="store_true",
+                    help="skip timing the exact ground-truth generation (pg_ground_truth)")
     ap.add_argument("--autotune", action="store_true",
                     help="run pg_autotune (launch shapes only; results unchanged) before timing")
     return ap.parse_args()
@@ -150,10 +152,10 @@ def allmax(x, world):
     return float(t.item())
 
 
-def gpu_workload(args, device):
+def gpu_workload(args, device, queries: bool = False):
     from paragraph_gb300 import datagen
-    base, gt = datagen.make_dataset_cuda(args.n, args.d, gt_k=128, seed=args.seed, device=device)
-    return base, gt
+    return datagen.make_dataset_cuda(args.n, args.d, gt_k=128, seed=args.seed, device=device,
+                                     return_queries=queries)
 
 
 def search_roofline(st, args, peak_gbs, peak_kind, rounds):
@@ -267,7 +269,10 @@ def run_ours(args):
     world, rank, local = dist_init(args)
     import paragraph_gb300 as pg
     dev = torch.device("cuda", local)
-    base, gt = gpu_workload(args, dev)
+    want_q = not args.no_gt
+    wl = gpu_workload(args, dev, queries=want_q)
+    base, gt = wl[0], wl[1]
+    queries = wl[2] if want_q else None
     torch.cuda.synchronize()
     screen = pg.SCREEN_BF16 if args.screen == "bf16" else pg.SCREEN_NONE
     params = pg.default_params(args.degree, args.beam, screen=screen)
@@ -344,6 +349,28 @@ def run_ours(args):
                       "mean_degree": round(float(kk.mean()), 3), "max_degree": int(kk.max()),
                       "params": "match_rounds 6, M_nn 40, M_final 70 (tests/test_t2iend.cu)"}
         del iout, icnt
+    # the build's input, ground truth top-128, generated exactly on the GPU (pg_ground_truth)
+    gt_line = None
+    if queries is not None:
+        gout = torch.empty((queries.shape[0], 128), dtype=torch.int32, device=dev)
+        h.ground_truth(base, queries[:1024], gout[:1024])  # cuBLAS and workspace set-up
+        torch.cuda.synchronize()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        h.ground_truth(base, queries, gout)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        gms = g0.elapsed_time(g1)
+        same = (gout == gt).all(dim=1).float().mean().item()
+        flop = 2.0 * queries.shape[0] * n * d
+        gt_line = {"ms": round(gms, 1), "queries": int(queries.shape[0]), "base": int(n),
+                   "k": 128, "screen_gemm_tflops_equiv": round(flop / (gms / 1e3) / 1e12, 1),
+                   "rows_equal_to_fp32_topk": round(same, 5),
+                   "definition": "exact FP64 inner products, ties to the lower id; the "
+                                 "benchmark's own ground truth is a float32 top-k"}
+        del gout, queries
+        torch.cuda.empty_cache()
     evals = stats[-1].evals_total
     assert all(s.evals_total == evals for s in stats), "evaluation count changed between builds"
     value = evals * args.steps * world / (ms_total / 1e3)
@@ -416,6 +443,7 @@ def run_ours(args):
                 "rescored": list(s.rescored)[:params.link_rounds],
                 "other_path": other_line,
                 "index": index_line,
+                "ground_truth": gt_line,
                 "gpu_launches": launches_per_build * args.steps,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary()}

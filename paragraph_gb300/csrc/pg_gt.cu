@@ -11,11 +11,11 @@
 //   3. a rigorous bound: |q.x - s^| <= E_q = (|q^| + |e_q|) max|e_x| + |e_q| max|x^|
 //      + g (|q^| max|x^|), with g covering the FP32 accumulation (d' * 2^-22, four times the
 //      IEEE unit roundoff, for the tensor core's accumulation);
-//   4. selection (k_gt_scan, up to eight warps per query row, one per row segment): a candidate
+//   4. selection (k_gt_scan, eight warps per query row, one per row segment): a candidate
 //      buffer that keeps every score >= (running k-th largest) - 2 E_q, compacted by a warp
-//      bitonic sort when full; then (k_gt_final) the row's k-th largest screened score t_k from
-//      the segments' first k entries, and the candidates with s^ >= t_k - 2 E_q from all of
-//      them, a superset of the true top-k;
+//      radix select when full; then (k_gt_final) the row's k-th largest screened score t_k
+//      over the segments' lists (radix select again), and the candidates with
+//      s^ >= t_k - 2 E_q, a superset of the true top-k;
 //   5. exact FP64 inner products of the candidates and a sort by (score desc, id asc).
 // On the benchmark's data a query keeps about 1.1 k candidates.
 #include <cublas_v2.h>
@@ -169,6 +169,137 @@ __device__ float compact_sorted(uint64_t* buf, uint32_t& cnt, uint32_t k, float 
   return theta;
 }
 
+// The k-th smallest of the keys' upper 32 bits (the k-th largest value) among buf[0 .. cnt),
+// by a four-pass 8-bit radix select with a 256-bin histogram in shared memory; loops, not an
+// unrolled network, so the scan kernel stays small.  Requires cnt >= k.
+__device__ uint32_t radix_kth(const uint64_t* buf, uint32_t cnt, uint32_t k, uint32_t* hist) {
+  const uint32_t lane = lane_id();
+  uint32_t prefix = 0, mask = 0, rem = k;
+  for (int shift = 24; shift >= 0; shift -= 8) {
+    for (uint32_t b = lane; b < 256; b += 32) hist[b] = 0;
+    __syncwarp();
+    for (uint32_t i = lane; i < cnt; i += 32) {
+      const uint32_t vk = static_cast<uint32_t>(buf[i] >> 32);
+      if ((vk & mask) == prefix) atomicAdd(hist + ((vk >> shift) & 255u), 1u);
+    }
+    __syncwarp();
+    uint32_t local[8], sum = 0;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      local[t] = hist[lane * 8 + t];
+      sum += local[t];
+    }
+    uint32_t incl = sum;  // inclusive scan of the lanes' sums
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= static_cast<uint32_t>(o)) incl += y;
+    }
+    const uint32_t excl = incl - sum;
+    const unsigned owner = __ballot_sync(kFull, excl < rem && rem <= incl);
+    const uint32_t src = static_cast<uint32_t>(__ffs(static_cast<int>(owner)) - 1);
+    uint32_t bin = 0, before = 0;
+    if (lane == src) {
+      uint32_t c = excl;
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        if (c + local[t] >= rem) {
+          bin = lane * 8 + t;
+          before = c;
+          break;
+        }
+        c += local[t];
+      }
+    }
+    bin = __shfl_sync(kFull, bin, src);
+    before = __shfl_sync(kFull, before, src);
+    prefix |= bin << shift;
+    mask |= 255u << shift;
+    rem -= before;
+    __syncwarp();
+  }
+  return prefix;
+}
+
+// radix_kth over the union of a row's segment lists in global memory (seg_keys / seg_cnt).
+__device__ uint32_t radix_kth_segs(const uint64_t* keys, const uint32_t* cnts, uint32_t segs,
+                                   uint32_t k, uint32_t* hist) {
+  const uint32_t lane = lane_id();
+  uint32_t prefix = 0, mask = 0, rem = k;
+  for (int shift = 24; shift >= 0; shift -= 8) {
+    for (uint32_t b = lane; b < 256; b += 32) hist[b] = 0;
+    __syncwarp();
+    for (uint32_t sg = 0; sg < segs; sg++) {
+      const uint64_t* src = keys + static_cast<uint64_t>(sg) * kGtCap;
+      const uint32_t c = cnts[sg];
+      for (uint32_t i = lane; i < c; i += 32) {
+        const uint32_t vk = static_cast<uint32_t>(src[i] >> 32);
+        if ((vk & mask) == prefix) atomicAdd(hist + ((vk >> shift) & 255u), 1u);
+      }
+    }
+    __syncwarp();
+    uint32_t local[8], sum = 0;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+      local[t] = hist[lane * 8 + t];
+      sum += local[t];
+    }
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= static_cast<uint32_t>(o)) incl += y;
+    }
+    const uint32_t excl = incl - sum;
+    const unsigned owner = __ballot_sync(kFull, excl < rem && rem <= incl);
+    const uint32_t src_lane = static_cast<uint32_t>(__ffs(static_cast<int>(owner)) - 1);
+    uint32_t bin = 0, before = 0;
+    if (lane == src_lane) {
+      uint32_t c = excl;
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        if (c + local[t] >= rem) {
+          bin = lane * 8 + t;
+          before = c;
+          break;
+        }
+        c += local[t];
+      }
+    }
+    bin = __shfl_sync(kFull, bin, src_lane);
+    before = __shfl_sync(kFull, before, src_lane);
+    prefix |= bin << shift;
+    mask |= 255u << shift;
+    rem -= before;
+    __syncwarp();
+  }
+  return prefix;
+}
+
+// Keeps (in place, order not kept) the entries of buf[0 .. cnt) whose value is >= the k-th
+// largest value minus band; returns that k-th largest value (-inf when cnt < k).
+__device__ float compact_select(uint64_t* buf, uint32_t& cnt, uint32_t k, float band,
+                                uint32_t* hist) {
+  const uint32_t lane = lane_id();
+  if (cnt < k) return -INFINITY;
+  const uint32_t kv = radix_kth(buf, cnt, k, hist);
+  const float theta = key_value(static_cast<uint64_t>(kv) << 32);
+  const float lo = theta - band;
+  uint32_t out = 0;
+  for (uint32_t i0 = 0; i0 < cnt; i0 += 32) {
+    const uint32_t i = i0 + lane;
+    const uint64_t key = i < cnt ? buf[i] : ~0ull;
+    const bool ok = i < cnt && key_value(key) >= lo;
+    const unsigned m = __ballot_sync(kFull, ok);
+    __syncwarp();
+    if (ok) buf[out + __popc(m & ((1u << lane) - 1u))] = key;
+    out += __popc(m);
+    __syncwarp();
+  }
+  cnt = out;
+  return theta;
+}
+
 __device__ float compact_any(uint64_t* buf, uint32_t& cnt, uint32_t k, float band) {
   if (cnt <= 128) return compact_sorted<4>(buf, cnt, k, band);
   if (cnt <= 256) return compact_sorted<8>(buf, cnt, k, band);
@@ -179,36 +310,64 @@ __device__ float compact_any(uint64_t* buf, uint32_t& cnt, uint32_t k, float ban
 // One warp per (query row, row segment): every screened score that may be in the top k.
 __global__ void __launch_bounds__(kScanWarps * 32) k_gt_scan(GtArgs a) {
   __shared__ uint64_t buf_all[kScanWarps][kGtCap];
+  __shared__ uint32_t hist_all[kScanWarps][256];
   uint64_t* buf = buf_all[threadIdx.x >> 5];
+  uint32_t* hist = hist_all[threadIdx.x >> 5];
   const uint32_t lane = lane_id();
   const uint64_t nw = static_cast<uint64_t>(gridDim.x) * kScanWarps;
-  const uint64_t seglen = (a.n + a.segs - 1) / a.segs;
+  // segments start on 512-value boundaries: one pass of the loop below reads 512 values per
+  // warp, 16 per lane as four 16-byte loads (when rows are 16-byte aligned, n % 4 == 0)
+  const uint64_t seglen = ((a.n + a.segs - 1) / a.segs + 511) & ~511ull;
+  const bool vec = (a.n & 3u) == 0;
   for (uint64_t w = blockIdx.x * static_cast<uint64_t>(kScanWarps) + (threadIdx.x >> 5);
        w < static_cast<uint64_t>(a.rows) * a.segs; w += nw) {
     const uint64_t row = w / a.segs, seg = w % a.segs;
-    const uint64_t x0 = seg * seglen, x1 = min(a.n, x0 + seglen);
+    const uint64_t x0 = min(a.n, seg * seglen), x1 = min(a.n, x0 + seglen);
     const float band = a.band[row];
     const float* srow = a.scores + row * a.n;
     uint32_t cnt = 0;
     float theta = -INFINITY;
     bool over = false;
-    for (uint64_t xb = x0; xb < x1 && !over; xb += 32) {
-      const uint64_t xi = xb + lane;
-      const float v = xi < x1 ? srow[xi] : -INFINITY;
-      bool pass = xi < x1 && v >= theta - band;
-      unsigned m = __ballot_sync(kFull, pass);
-      if (cnt + __popc(m) > kGtCap) {
-        theta = compact_any(buf, cnt, a.k, band);
-        pass = xi < x1 && v >= theta - band;
-        m = __ballot_sync(kFull, pass);
-        if (cnt + __popc(m) > kGtCap) {
-          over = true;
-          break;
+    for (uint64_t xb = x0; xb < x1 && !over; xb += 512) {
+      float v[16];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const uint64_t p = xb + 128u * j + 4u * lane;
+        if (vec && p + 3 < x1) {
+          const float4 f = __ldg(reinterpret_cast<const float4*>(srow + p));
+          v[4 * j] = f.x;
+          v[4 * j + 1] = f.y;
+          v[4 * j + 2] = f.z;
+          v[4 * j + 3] = f.w;
+        } else {
+#pragma unroll
+          for (int t = 0; t < 4; t++) v[4 * j + t] = p + t < x1 ? srow[p + t] : -INFINITY;
         }
       }
-      if (pass) buf[cnt + __popc(m & ((1u << lane) - 1u))] = desc_key(v, static_cast<uint32_t>(xi));
-      cnt += __popc(m);
-      __syncwarp();
+      float mx = v[0];
+#pragma unroll
+      for (int j = 1; j < 16; j++) mx = fmaxf(mx, v[j]);
+      if (!__any_sync(kFull, mx >= theta - band)) continue;  // the common case once warm
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        const uint64_t xi = xb + 128u * (j >> 2) + 4u * lane + (j & 3);
+        bool pass = xi < x1 && v[j] >= theta - band;
+        unsigned m = __ballot_sync(kFull, pass);
+        if (!m) continue;
+        if (cnt + __popc(m) > kGtCap) {
+          theta = compact_select(buf, cnt, a.k, band, hist);
+          pass = xi < x1 && v[j] >= theta - band;
+          m = __ballot_sync(kFull, pass);
+          if (cnt + __popc(m) > kGtCap) {
+            over = true;
+            break;
+          }
+        }
+        if (pass)
+          buf[cnt + __popc(m & ((1u << lane) - 1u))] = desc_key(v[j], static_cast<uint32_t>(xi));
+        cnt += __popc(m);
+        __syncwarp();
+      }
     }
     if (over) {
       if (lane == 0) {
@@ -218,7 +377,7 @@ __global__ void __launch_bounds__(kScanWarps * 32) k_gt_scan(GtArgs a) {
       }
       continue;
     }
-    theta = compact_any(buf, cnt, a.k, band);
+    theta = compact_select(buf, cnt, a.k, band, hist);
     uint64_t* dst = a.seg_keys + w * kGtCap;
     for (uint32_t i = lane; i < cnt; i += 32) dst[i] = buf[i];
     if (lane == 0) {
@@ -299,6 +458,8 @@ __device__ void rescore_write(const GtArgs& a, uint64_t row, const uint64_t* buf
 __global__ void __launch_bounds__(kFinalWarps * 32) k_gt_final(GtArgs a) {
   __shared__ uint64_t buf_all[kFinalWarps][kGtCap];
   __shared__ uint32_t ids_all[kFinalWarps][kGtCap];
+  __shared__ uint32_t hist_all[kFinalWarps][256];
+  uint32_t* hist = hist_all[threadIdx.x >> 5];
   uint64_t* buf = buf_all[threadIdx.x >> 5];
   uint32_t* ids_s = ids_all[threadIdx.x >> 5];
   const uint32_t lane = lane_id();
@@ -306,21 +467,19 @@ __global__ void __launch_bounds__(kFinalWarps * 32) k_gt_final(GtArgs a) {
   for (uint64_t row = blockIdx.x * static_cast<uint64_t>(kFinalWarps) + (threadIdx.x >> 5);
        row < a.rows; row += nw) {
     const float band = a.band[row];
-    // pass 1: the row's k-th largest screened score t_k, from the first k entries of every
-    // segment (each segment's list is sorted best first and holds its own top k)
-    uint32_t cnt = 0;
-    for (uint32_t s = 0; s < a.segs; s++) {
-      const uint64_t w = row * a.segs + s;
-      const uint32_t c = min(a.seg_cnt[w], a.k);
-      const uint64_t* src = a.seg_keys + w * kGtCap;
-      for (uint32_t i = lane; i < c; i += 32) buf[cnt + i] = src[i];
-      cnt += c;
-    }
-    __syncwarp();
-    const float tk = compact_any(buf, cnt, a.k, 0.0f);
+    // pass 1: the row's k-th largest screened score t_k over the union of the segment lists
+    // (each holds its own segment's top k)
+    uint32_t total = 0;
+    for (uint32_t s = 0; s < a.segs; s++) total += a.seg_cnt[row * a.segs + s];
+    const float tk = total >= a.k
+                         ? key_value(static_cast<uint64_t>(radix_kth_segs(
+                                         a.seg_keys + row * a.segs * kGtCap,
+                                         a.seg_cnt + row * a.segs, a.segs, a.k, hist))
+                                     << 32)
+                         : -INFINITY;
     // pass 2: every screened score >= t_k - band, from the whole segment lists
     const float lo = tk - band;
-    cnt = 0;
+    uint32_t cnt = 0;
     bool over = false;
     for (uint32_t s = 0; s < a.segs && !over; s++) {
       const uint64_t w = row * a.segs + s;
@@ -386,8 +545,8 @@ size_t gt_workspace_bytes(uint64_t n, uint64_t nq, uint32_t d, uint32_t segs) {
 int ground_truth(cublasContext* blas, const float* base, uint64_t n, uint32_t d,
                  const float* queries, uint64_t nq, uint32_t k, uint32_t* out, char* ws,
                  uint32_t* status, int num_sms, cudaStream_t st, float* diag) {
-  // segments per row: their first k entries must fit one candidate buffer (kGtCap)
-  const uint32_t kSegs = max(1u, min(8u, kGtCap / k));
+  // segments per row (each keeps its own top k plus the margin in a kGtCap buffer)
+  const uint32_t kSegs = 8;
   const uint64_t cq = gt_chunk_rows(n, nq);
   auto al = [](uint64_t b) { return (b + 255) & ~255ull; };
   char* p = ws;

@@ -75,9 +75,9 @@ def make_dataset(n: int, d: int, q: int | None = None, gt_k: int = 128, seed: in
 def make_dataset_cuda(n: int, d: int, q: int | None = None, gt_k: int = 128, centers: int = 64,
                       sigma: float = 0.3, query_scale: float = 0.6, shift_norm: float = 2.0,
                       noise: float = 0.2, cosine: bool = False, seed: int = 1234,
-                      chunk: int = 4096, device: str = "cuda"):
+                      chunk: int = 4096, device: str = "cuda", return_queries: bool = False):
     """The same recipe on the GPU with torch (for N in the millions).  Returns device tensors
-    (base float32 N x D, gt int32 viewed as uint32 Q x gt_k)."""
+    (base float32 N x D, gt int32 viewed as uint32 Q x gt_k[, queries float32 Q x D])."""
     import torch
 
     q = n if q is None else q
@@ -111,5 +111,7 @@ def make_dataset_cuda(n: int, d: int, q: int | None = None, gt_k: int = 128, cen
             del sc, vals, idx
     finally:
         torch.backends.cuda.matmul.allow_tf32 = prev
+    if return_queries:
+        return base.contiguous(), gt, queries.contiguous()
     del queries
     return base.contiguous(), gt
