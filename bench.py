@@ -56,6 +56,14 @@ def parse():
     ap.add_argument("--no-index", action="store_true",
                     help="skip timing the whole index (pg_build_index: build + RoarGraph path + "
                          "FusionFinal)")
+    ap.add_argument("--cosine", action="store_true",
+                    help="L2-normalise base and queries (cosine = inner product)")
+    ap.add_argument("--centers", type=int, default=64, help="mixture components")
+    ap.add_argument("--batched", type=int, default=0, metavar="S",
+                    help="batched form: S sub-indexes of log-uniform sizes in "
+                         "[--min-points, --max-points], one build for all against one by one")
+    ap.add_argument("--min-points", type=int, default=10_000)
+    ap.add_argument("--max-points", type=int, default=500_000)
     ap.add_argument("--no-gt", action="store_true",
                     help="skip timing the exact ground-truth generation (pg_ground_truth)")
     ap.add_argument("--autotune", action="store_true",
@@ -155,7 +163,8 @@ def allmax(x, world):
 def gpu_workload(args, device, queries: bool = False):
     from paragraph_gb300 import datagen
     return datagen.make_dataset_cuda(args.n, args.d, gt_k=128, seed=args.seed, device=device,
-                                     return_queries=queries)
+                                     return_queries=queries, cosine=args.cosine,
+                                     centers=args.centers)
 
 
 def search_roofline(st, args, peak_gbs, peak_kind, rounds):
@@ -455,10 +464,106 @@ def run_ours(args):
     return 0
 
 
+def run_batched(args):
+    """Batched form: S independent sub-indexes of uneven (seeded log-uniform) sizes, each with its
+    own training queries (Q = N) and exact top-128 ground truth (pg_ground_truth), built in one
+    CUDA-graph-captured pass (pg_build_batched_device) against building them one by one."""
+    import numpy as np
+    import torch
+    import paragraph_gb300 as pg
+    from paragraph_gb300 import datagen
+    dev = torch.device("cuda", 0)
+    rng = np.random.Generator(np.random.PCG64(args.seed))
+    sizes = np.exp(rng.uniform(np.log(args.min_points), np.log(args.max_points),
+                               args.batched)).astype(np.int64)
+    node_off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    total = int(node_off[-1])
+    base = torch.empty((total, args.d), dtype=torch.float32, device=dev)
+    gt = torch.empty((total, 128), dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(dev)
+    h = pg.Handle(0, stream=stream)
+    t0 = time.perf_counter()
+    gt_ms = 0.0
+    for i, ni in enumerate(sizes):
+        lo, hi = int(node_off[i]), int(node_off[i + 1])
+        b, _, q = datagen.make_dataset_cuda(int(ni), args.d, seed=args.seed + 1 + i, device=dev,
+                                            cosine=args.cosine, centers=args.centers,
+                                            with_gt=False)
+        base[lo:hi] = b
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        h.ground_truth(b, q, gt[lo:hi])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        gt_ms += e0.elapsed_time(e1)
+        del b, q
+    torch.cuda.empty_cache()
+    gen_s = time.perf_counter() - t0
+    screen = pg.SCREEN_BF16 if args.screen == "bf16" else pg.SCREEN_NONE
+    params = pg.default_params(args.degree, args.beam, screen=screen, flags=pg.FLAG_CUDA_GRAPH)
+    tuning = None
+    if args.autotune:
+        _, tun = h.autotune(base, gt, params, node_off=node_off, query_off=node_off)
+        tuning = tun.as_dict()
+    graph = torch.empty((total, args.degree), dtype=torch.int32, device=dev)
+    for _ in range(args.warmup):
+        st = h.build_batched(base, gt, node_off, node_off, graph, None, params)
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clocks:
+        a = torch.cuda.Event(enable_timing=True)
+        b_ = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            st = h.build_batched(base, gt, node_off, node_off, graph, None, params)
+        b_.record(stream)
+        torch.cuda.synchronize()
+    ms = a.elapsed_time(b_) / args.steps
+    # one by one, same parameters, no graph
+    p1 = pg.default_params(args.degree, args.beam, screen=screen)
+    alone = torch.empty_like(graph)
+    for i, ni in enumerate(sizes):  # warm-up
+        lo, hi = int(node_off[i]), int(node_off[i + 1])
+        h.build_device(base[lo:hi], gt[lo:hi], alone[lo:hi], None, p1)
+    torch.cuda.synchronize()
+    a.record(stream)
+    ev_alone = 0
+    for i, ni in enumerate(sizes):
+        lo, hi = int(node_off[i]), int(node_off[i + 1])
+        ev_alone += h.build_device(base[lo:hi], gt[lo:hi], alone[lo:hi], None, p1).evals_total
+    b_.record(stream)
+    torch.cuda.synchronize()
+    ms_alone = a.elapsed_time(b_)
+    identical = bool(torch.equal(graph, alone))
+    line = {"metric": METRIC + " -- batched form", "value": st.evals_total / (ms / 1e3),
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.screen == "none" else "f32+bf16",
+            "data": "synthetic (seeded mixture-of-Gaussians, one set per sub-index)",
+            "config": {"workload": f"{args.batched} sub-indexes, sizes log-uniform in "
+                                   f"[{args.min_points}, {args.max_points}] (total {total}), "
+                                   f"D={args.d}, {'cosine' if args.cosine else 'IP'}, "
+                                   f"M={args.degree}, L={args.beam}, one CUDA-graph replay",
+                       "sizes_min_max": [int(sizes.min()), int(sizes.max())], "total": total},
+            "one_by_one": {"ms": round(ms_alone, 3), "evals": int(ev_alone),
+                           "identical_edges": identical,
+                           "speedup_of_batched": round(ms_alone / ms, 3)},
+            "ground_truth": {"ms_total": round(gt_ms, 1), "k": 128,
+                             "definition": "exact FP64 inner products (pg_ground_truth)"},
+            "data_generation_s": round(gen_s, 1), "tuning": tuning,
+            "gpu_launches": (10 + 8 * params.link_rounds) * args.steps, "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+    h.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.batched:
+        return run_batched(args)
     return run_ours(args)
 
 

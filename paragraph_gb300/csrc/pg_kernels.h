@@ -173,7 +173,6 @@ bool screen_supported(uint32_t c, uint32_t d, int strict);
 size_t screen_smem_per_warp(uint32_t d);
 cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_optin,
                                 cudaStream_t st);
-size_t search_smem_per_warp(uint32_t d, uint32_t hash_slots);
 
 constexpr uint32_t kScanTileElems = 4096;
 

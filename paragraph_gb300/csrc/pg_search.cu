@@ -121,260 +121,22 @@ struct Q4 {
   float4 v[NS];
 };
 
-// Stage the rows of this warp's new candidates into shared memory and return this lane's
-// distance (FLT_MAX where newc is false).  Returns false in *ok when the bounded wait failed.
-template <int KSTEPS>
-__device__ __forceinline__ float stage_and_score(const SearchArgs& a, const Q4<KSTEPS>& q,
-                                                 uint32_t node, bool newc, float* rows,
-                                                 uint64_t* mbar, uint32_t& phase, bool& ok) {
-  const uint32_t lane = lane_id();
-  const unsigned newmask = __ballot_sync(kFull, newc);
-  const uint32_t nnew = __popc(newmask);
-  if (nnew == 0) return FLT_MAX;
-  const uint32_t d = a.d;
-  const uint32_t ci = __popc(newmask & ((1u << lane) - 1u));  // compact slot of this lane
-  fence_proxy_async();
-  if (lane == 0) mbar_arrive_expect_tx(mbar, nnew * d * 4u);
-  __syncwarp();
-  if (newc)
-    bulk_row_to_smem(rows + static_cast<size_t>(ci) * d, a.base + static_cast<uint64_t>(node) * d,
-                     d * 4u, mbar);
-  ok = mbar_wait_bounded(mbar, phase);
-  phase ^= 1u;
-  if (!ok) return FLT_MAX;
-
-  const uint32_t g = lane >> 3, m = lane & 7u;
-  float p[8][4];
-#pragma unroll
-  for (int r = 0; r < 8; r++)
-#pragma unroll
-    for (int i = 0; i < 4; i++) p[r][i] = 0.0f;
-#pragma unroll
-  for (int r = 0; r < 8; r++) {
-    if (4u * r < nnew) {
-      const uint32_t c = 4u * r + g;
-      if (c < nnew) {
-        const float* row = rows + static_cast<size_t>(c) * d;
-#pragma unroll
-        for (int k = 0; k < KSTEPS; k++) {
-          const uint32_t off = 32u * k + 4u * m;
-          if (off < d) {
-            const float4 x = *reinterpret_cast<const float4*>(row + off);
-            p[r][0] = fmaf(q.v[k].x, x.x, p[r][0]);
-            p[r][1] = fmaf(q.v[k].y, x.y, p[r][1]);
-            p[r][2] = fmaf(q.v[k].z, x.z, p[r][2]);
-            p[r][3] = fmaf(q.v[k].w, x.w, p[r][3]);
-          }
-        }
-      }
-    }
-  }
-  // transposed shuffle tree: xor 4 (residues +16), xor 2 (+8), xor 1 (+4)
-  const bool bA = (m & 4u) != 0, bB = (m & 2u) != 0, bC = (m & 1u) != 0;
-  float a4[4][4];
-#pragma unroll
-  for (int i = 0; i < 4; i++)
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const float send = bA ? p[i][j] : p[i + 4][j];
-      const float keep = bA ? p[i + 4][j] : p[i][j];
-      a4[i][j] = keep + __shfl_xor_sync(kFull, send, 4);
-    }
-  float b2[2][4];
-#pragma unroll
-  for (int i = 0; i < 2; i++)
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const float send = bB ? a4[i][j] : a4[i + 2][j];
-      const float keep = bB ? a4[i + 2][j] : a4[i][j];
-      b2[i][j] = keep + __shfl_xor_sync(kFull, send, 2);
-    }
-  float v[4];
-#pragma unroll
-  for (int j = 0; j < 4; j++) {
-    const float send = bC ? b2[0][j] : b2[1][j];
-    const float keep = bC ? b2[1][j] : b2[0][j];
-    v[j] = keep + __shfl_xor_sync(kFull, send, 1);
-  }
-  const float total = (v[0] + v[2]) + (v[1] + v[3]);  // levels 2 and 1 of the tree
-  // lane (g, m) holds candidate 4m + g; route it to the lane that owns that candidate
-  const uint32_t src = newc ? (((ci & 3u) << 3) | (ci >> 2)) : 0u;
-  const float dist = -__shfl_sync(kFull, total, src);
-  return newc ? dist : FLT_MAX;
-}
-
 }  // namespace
 
-template <int KM_S, int KSTEPS>
-__global__ void __launch_bounds__(32) k_search(SearchArgs a) {
-  constexpr int E = (KM_S + 1 <= 2) ? 2 : 4;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const uint32_t lane = lane_id();
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw);
-  uint32_t* hash = reinterpret_cast<uint32_t*>(smem_raw + 16);
-  float* rows = reinterpret_cast<float*>(smem_raw + 16 + 4u * a.hash_slots);
-  const uint32_t hmask = a.hash_slots - 1u;
-  const uint32_t km = a.km, kp = a.kp, kd = a.kd;
-  const uint32_t L = km + 32u;
-  if (lane == 0) mbar_init(mbar, 1);
-  __syncwarp();
-  uint32_t phase = 0;
-  unsigned long long ev = 0, it_all = 0;
-  bool ok = true;
-  const uint32_t g = lane >> 3, m = lane & 7u;
-  const uint32_t e_of_lane = lane / kd, nb_of_lane = lane % kd;
-
-  for (;;) {
-    uint32_t qi = 0;
-    if (lane == 0) qi = atomicAdd(a.work, 1u);
-    qi = __shfl_sync(kFull, qi, 0);
-    if (qi >= (a.queries ? a.nq : a.n)) break;
-    const uint32_t qid = a.order ? a.order[qi] : qi;
-    const float* qrow = (a.queries ? a.queries : a.base) + static_cast<uint64_t>(qid) * a.d;
-    Q4<KSTEPS> q;
-#pragma unroll
-    for (int k = 0; k < KSTEPS; k++) {
-      const uint32_t off = 32u * k + 4u * m;
-      q.v[k] = (off < a.d) ? __ldg(reinterpret_cast<const float4*>(qrow + off))
-                           : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    (void)g;
-    uint64_t key[E];
-    uint32_t id[E];
-#pragma unroll
-    for (int s = 0; s < E; s++) {
-      key[s] = ~0ull;
-      id[s] = kTomb;
-    }
-#pragma unroll
-    for (int s = 0; s < KM_S; s++) key[s] = pack_key(FLT_MAX, static_cast<uint32_t>(s) * 32u + lane);
-
-    // seeds: every slot is scored (Gsearcher.cuh:958-976 has no visited test)
-    {
-      uint64_t soff = 0, sn = a.n;  // entry points are drawn inside the query's sub-index
-      if (a.seg_count) {
-        const uint32_t sg = segment_of(a.seg_off, a.seg_count, qid);
-        soff = a.seg_off[sg];
-        sn = a.seg_off[sg + 1] - soff;
-      }
-      const uint32_t node =
-          static_cast<uint32_t>((a.seed_base + static_cast<uint64_t>(lane)) % sn + soff);
-      const float dist = stage_and_score<KSTEPS>(a, q, node, true, rows, mbar, phase, ok);
-      if (!ok) break;
-      key[KM_S] = pack_key(dist, km + lane);
-      id[KM_S] = node;
-      ev += (lane == 0) ? 32u : 0u;
-    }
-    warp_sort_kv<E>(key, id);
-    hash_clear(hash, a.hash_slots);
-    __syncwarp();
-#pragma unroll
-    for (int s = 0; s < KM_S; s++) hash_insert(hash, hmask, id[s] & kMaskedTomb);
-    __syncwarp();
-
-    uint32_t iter = 0, total = 0;
-    for (;;) {
-      // collect_top_p_normal: first kp unexplored of the top km, mark them explored
-      uint32_t found = 0;
-      uint32_t ex_lane = kTomb;  // lane e holds explore id e
-#pragma unroll
-      for (int s = 0; s < KM_S; s++) {
-        if (found < kp) {
-          const bool unexp = (id[s] & kParent) == 0;
-          const unsigned mask = __ballot_sync(kFull, unexp);
-          const uint32_t cnt = __popc(mask);
-          const uint32_t rank = __popc(mask & ((1u << lane) - 1u));
-          const bool want = lane >= found && lane < found + cnt && lane < kp;
-          uint32_t src = 0;
-          if (want) {  // position of set bit number (lane - found) of mask
-            unsigned mm = mask;
-            for (uint32_t i = found; i < lane; i++) mm &= mm - 1u;
-            src = static_cast<uint32_t>(__ffs(static_cast<int>(mm)) - 1);
-          }
-          const uint32_t got = __shfl_sync(kFull, id[s], src);
-          if (want) ex_lane = got;
-          if (unexp && found + rank < kp) id[s] |= kParent;
-          found += cnt;
-        }
-      }
-      if (found == 0) break;
-      if (++total > a.max_iters) {
-        if (lane == 0) raise_error(a.status, kErrIterCap);
-        break;
-      }
-      const uint32_t ex = __shfl_sync(kFull, ex_lane, e_of_lane);
-      uint32_t node = kTomb;
-      if (ex < a.n)
-        node = a.graph[static_cast<uint64_t>(ex) * a.graph_degree + nb_of_lane];
-      else if (ex != kTomb)
-        raise_error(a.status, kErrCapacity);  // not reachable: list ids are < n or tomb
-      if (node >= a.n && node != kTomb) {  // out-of-range graph entry
-        raise_error(a.status, kErrBadId);
-        node = kTomb;
-      }
-      const bool valid = node != kTomb;
-      const unsigned same = __match_any_sync(kFull, node);
-      const bool first = lane == static_cast<uint32_t>(__ffs(static_cast<int>(same)) - 1);
-      const bool newc = valid && first && !hash_contains(hash, hmask, node);
-      __syncwarp();
-      if (newc) hash_insert(hash, hmask, node);
-      __syncwarp();
-      const float dist = stage_and_score<KSTEPS>(a, q, node, newc, rows, mbar, phase, ok);
-      if (!ok) break;
-      const unsigned scored = __ballot_sync(kFull, newc);  // every lane takes part
-      ev += (lane == 0) ? __popc(scored) : 0u;
-#pragma unroll
-      for (int s = 0; s < KM_S; s++)
-        key[s] = (key[s] & 0xFFFFFFFF00000000ull) | (static_cast<uint32_t>(s) * 32u + lane);
-      key[KM_S] = pack_key(dist, km + lane);
-      id[KM_S] = node;
-#pragma unroll
-      for (int s = KM_S + 1; s < E; s++) {
-        key[s] = ~0ull;
-        id[s] = kTomb;
-      }
-      warp_sort_kv<E>(key, id);
-      if (++iter == a.reset_iter) {
-        hash_clear(hash, a.hash_slots);
-        __syncwarp();
-#pragma unroll
-        for (int s = 0; s < KM_S; s++) hash_insert(hash, hmask, id[s] & kMaskedTomb);
-        __syncwarp();
-        iter = 0;
-      }
-    }
-    if (!ok) break;
-    it_all += (lane == 0) ? total : 0u;
-    uint32_t* orow = a.out + static_cast<uint64_t>(qid) * a.out_width;
-#pragma unroll
-    for (int s = 0; s < E; s++) {
-      const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
-      if (i < L && i < a.out_width) orow[i] = id[s] & kMaskedTomb;
-    }
-  }
-  if (!ok) {
-    if (lane == 0) raise_error(a.status, kErrWait);
-    mbar_wait_bounded(mbar, phase ^ 1u);  // let a late copy land before the block exits
-  }
-  if (lane == 0) {
-    if (ev) atomicAdd(a.evals, ev);
-    if (it_all) atomicAdd(a.iters, it_all);
-  }
-}
-
 // ---------------------------------------------------------------------------------------------
-// Km = 32 path (one retained entry per lane).  Differences from k_search above:
-//   * candidate rows are staged ROWS at a time (ROWS*D*4 bytes of shared memory instead of 32
-//     rows), so several times more warps stay resident;
-//   * the sorted top 32 is kept in registers and the new candidates are merged into it by rank
+// The search kernels (k_search_m32 for Km = 32, k_search_mk for Km = 64, 96):
+//   * candidate rows are staged ROWS at a time (ROWS*D*4 bytes of shared memory), so many warps
+//     stay resident;
+//   * the sorted top Km is kept in registers and the new candidates are merged into it by rank
 //     (ballot/popc against unique (distance, position) keys) -- the same total order as sorting
-//     the whole list, without the 64-key network every iteration;
-//   * the full 64-entry list (top before the last merge + the last candidates) is sorted once,
+//     the whole list, without a sorting network every iteration;
+//   * the full L-entry list (top before the last merge + the last candidates) is sorted once,
 //     when the query ends, for the output.
 namespace {
 
-// Scores the lanes whose `newc` is set, ROWS rows per pass (see stage_and_score for the FP32
-// order).  ROUNDS = ROWS/4 candidates per 8-lane group; the first log2(ROUNDS) butterfly levels
+// Scores the lanes whose `newc` is set, ROWS rows per pass.  Lane (g, m) = (lane / 8, lane % 8)
+// accumulates residues 4m..4m+3 of candidate rows 4r + g (the reference's lane-strided FMA
+// chains, one 16-byte shared load per 32 elements).  ROUNDS = ROWS/4 candidates per 8-lane group; the first log2(ROUNDS) butterfly levels
 // are transposed (each lane keeps one candidate), the remaining ones are plain xor reductions.
 template <int KSTEPS, int ROWS>
 __device__ __forceinline__ float score_passes(const SearchArgs& a, const Q4<KSTEPS>& q,
@@ -667,6 +429,273 @@ __global__ void __launch_bounds__(32, KSTEPS <= 8 ? 20 : 12) k_search_m32(Search
   }
 }
 
+// k_search_m32 generalised to Km = 32 * KM_S (64, 96): the top-Km list in KM_S register slots
+// (element i in lane i % 32, slot i / 32), the same candidate staging and FP32 order, the rank
+// merge of the scored candidates over all slots, one bitonic sort of the final list.
+template <int KM_S, int KSTEPS, int ROWS>
+__global__ void __launch_bounds__(32, KSTEPS <= 8 ? 16 : 8) k_search_mk(SearchArgs a) {
+  constexpr int EF = (KM_S + 1 <= 2) ? 2 : 4;  // final sort: KM_S + 1 slots, padded to 2^k
+  constexpr uint32_t KM = 32u * KM_S;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const uint32_t lane = lane_id();
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw);
+  uint64_t* mkey = reinterpret_cast<uint64_t*>(smem_raw + 16);      // KM merge keys
+  uint32_t* mid = reinterpret_cast<uint32_t*>(smem_raw + 16 + 8 * KM);  // KM merge ids
+  uint32_t* hash = reinterpret_cast<uint32_t*>(smem_raw + 16 + 12 * KM);
+  float* rows = reinterpret_cast<float*>(smem_raw + 16 + 12 * KM + 4u * a.hash_slots);
+  const uint32_t hmask = a.hash_slots - 1u;
+  const uint32_t kp = a.kp, kd = a.kd;
+  if (lane == 0) mbar_init(mbar, 1);
+  __syncwarp();
+  uint32_t phase = 0;
+  unsigned long long ev = 0, it_all = 0;
+  bool ok = true;
+  const uint32_t m = lane & 7u;
+  const uint32_t e_of_lane = lane / kd, nb_of_lane = lane % kd;
+  const unsigned lt_mask = (1u << lane) - 1u;
+
+  for (;;) {
+    uint32_t qi = 0;
+    if (lane == 0) qi = atomicAdd(a.work, 1u);
+    qi = __shfl_sync(kFull, qi, 0);
+    if (qi >= (a.queries ? a.nq : a.n)) break;
+    const uint32_t qid = a.order ? a.order[qi] : qi;
+    const float* qrow = (a.queries ? a.queries : a.base) + static_cast<uint64_t>(qid) * a.d;
+    Q4<KSTEPS> q;
+#pragma unroll
+    for (int k = 0; k < KSTEPS; k++) {
+      const uint32_t off = 32u * k + 4u * m;
+      q.v[k] = (off < a.d) ? __ldg(reinterpret_cast<const float4*>(qrow + off))
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    uint64_t top_key[KM_S];
+    uint32_t top_id[KM_S];
+#pragma unroll
+    for (int s = 0; s < KM_S; s++) {
+      top_key[s] = pack_key(FLT_MAX, static_cast<uint32_t>(s) * 32u + lane);
+      top_id[s] = kTomb;
+    }
+    uint64_t cand_key;
+    uint32_t cand_id;
+    {  // seeds (Gsearcher.cuh:958-976 has no visited test)
+      uint64_t soff = 0, sn = a.n;
+      if (a.seg_count) {
+        const uint32_t sg = segment_of(a.seg_off, a.seg_count, qid);
+        soff = a.seg_off[sg];
+        sn = a.seg_off[sg + 1] - soff;
+      }
+      const uint32_t node =
+          static_cast<uint32_t>((a.seed_base + static_cast<uint64_t>(lane)) % sn + soff);
+      const float dist = score_passes<KSTEPS, ROWS>(a, q, node, true, rows, mbar, phase, ok);
+      if (!ok) break;
+      cand_key = pack_key(dist, KM + lane);
+      cand_id = node;
+      ev += (lane == 0) ? 32u : 0u;
+    }
+    uint64_t cur_key[KM_S];
+    uint32_t cur_id[KM_S];
+    {
+      uint64_t k2[EF];
+      uint32_t i2[EF];
+#pragma unroll
+      for (int s = 0; s < EF; s++) {
+        k2[s] = s < KM_S ? top_key[s < KM_S ? s : 0] : (s == KM_S ? cand_key : ~0ull);
+        i2[s] = s < KM_S ? top_id[s < KM_S ? s : 0] : (s == KM_S ? cand_id : kTomb);
+      }
+      warp_sort_kv<EF>(k2, i2);
+#pragma unroll
+      for (int s = 0; s < KM_S; s++) {
+        cur_key[s] = k2[s];
+        cur_id[s] = i2[s];
+      }
+    }
+    hash_clear(hash, a.hash_slots);
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < KM_S; s++) hash_insert(hash, hmask, cur_id[s] & kMaskedTomb);
+    __syncwarp();
+
+    uint32_t iter = 0, total = 0;
+    for (;;) {
+      // collect_top_p_normal: the first kp unexplored of the top Km, marked explored
+      unsigned um[KM_S];
+      uint32_t found = 0;
+#pragma unroll
+      for (int s = 0; s < KM_S; s++) {
+        um[s] = __ballot_sync(kFull, (cur_id[s] & kParent) == 0);
+        found += __popc(um[s]);
+      }
+      if (found == 0) break;
+      int want_slot = -1;
+      uint32_t want_src = 0;
+      if (lane < kp && lane < found) {
+        uint32_t r = lane;
+#pragma unroll
+        for (int s = 0; s < KM_S; s++) {
+          const uint32_t c = __popc(um[s]);
+          if (want_slot < 0) {
+            if (r < c) {
+              unsigned mm = um[s];
+              for (uint32_t i = 0; i < r; i++) mm &= mm - 1u;
+              want_src = static_cast<uint32_t>(__ffs(static_cast<int>(mm)) - 1);
+              want_slot = s;
+            } else {
+              r -= c;
+            }
+          }
+        }
+      }
+      uint32_t ex_lane = kTomb;
+#pragma unroll
+      for (int s = 0; s < KM_S; s++) {
+        const uint32_t v = __shfl_sync(kFull, cur_id[s], want_src);
+        if (want_slot == s) ex_lane = v;
+      }
+      {
+        uint32_t before = 0;
+#pragma unroll
+        for (int s = 0; s < KM_S; s++) {
+          const uint32_t rank = before + __popc(um[s] & lt_mask);
+          if ((cur_id[s] & kParent) == 0 && rank < kp) cur_id[s] |= kParent;
+          before += __popc(um[s]);
+        }
+      }
+      if (++total > a.max_iters) {
+        if (lane == 0) raise_error(a.status, kErrIterCap);
+        break;  // the output is the list of the last completed merge
+      }
+      const uint32_t ex = __shfl_sync(kFull, ex_lane, e_of_lane);
+      uint32_t node = kTomb;
+      if (ex < a.n)
+        node = a.graph[static_cast<uint64_t>(ex) * a.graph_degree + nb_of_lane];
+      else if (ex != kTomb)
+        raise_error(a.status, kErrCapacity);
+      if (node >= a.n && node != kTomb) {
+        raise_error(a.status, kErrBadId);
+        node = kTomb;
+      }
+      const bool valid = node != kTomb;
+      const unsigned same = __match_any_sync(kFull, node);
+      const bool first = lane == static_cast<uint32_t>(__ffs(static_cast<int>(same)) - 1);
+      const bool newc = valid && first && !hash_contains(hash, hmask, node);
+      __syncwarp();
+      if (newc) hash_insert(hash, hmask, node);
+      __syncwarp();
+      const float dist = score_passes<KSTEPS, ROWS>(a, q, node, newc, rows, mbar, phase, ok);
+      if (!ok) break;
+      const unsigned scored = __ballot_sync(kFull, newc);
+      ev += (lane == 0) ? __popc(scored) : 0u;
+      // the list this merge sorts: top (positions 0..Km-1) + candidates (Km..Km+31)
+#pragma unroll
+      for (int s = 0; s < KM_S; s++) {
+        top_key[s] = (cur_key[s] & 0xFFFFFFFF00000000ull) | (static_cast<uint32_t>(s) * 32u + lane);
+        top_id[s] = cur_id[s];
+      }
+      cand_key = pack_key(newc ? dist : FLT_MAX, KM + lane);
+      cand_id = node;
+      // rank merge of the candidates below the current Km-th key (see k_search_m32)
+      const uint64_t worst = __shfl_sync(kFull, top_key[KM_S - 1], 31);
+      uint32_t shift[KM_S];
+#pragma unroll
+      for (int s = 0; s < KM_S; s++) shift[s] = 0;
+      uint32_t cpos = 0xFFFFFFFFu;
+      unsigned rem = __ballot_sync(kFull, newc && cand_key < worst);
+      while (rem) {
+        const uint32_t c = static_cast<uint32_t>(__ffs(static_cast<int>(rem)) - 1);
+        rem &= rem - 1u;
+        const uint64_t kc = __shfl_sync(kFull, cand_key, c);
+        uint32_t below_top = 0;
+#pragma unroll
+        for (int s = 0; s < KM_S; s++) {
+          below_top += __popc(__ballot_sync(kFull, top_key[s] < kc));
+          shift[s] += (top_key[s] > kc) ? 1u : 0u;
+        }
+        const uint32_t below_cand = __popc(__ballot_sync(kFull, newc && cand_key < kc));
+        if (lane == c) cpos = below_top + below_cand;
+      }
+#pragma unroll
+      for (int s = 0; s < KM_S; s++) {
+        const uint32_t tpos = static_cast<uint32_t>(s) * 32u + lane + shift[s];
+        if (tpos < KM) {
+          mkey[tpos] = top_key[s];
+          mid[tpos] = top_id[s];
+        }
+      }
+      if (cpos < KM) {
+        mkey[cpos] = cand_key;
+        mid[cpos] = cand_id;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int s = 0; s < KM_S; s++) {
+        cur_key[s] = mkey[static_cast<uint32_t>(s) * 32u + lane];
+        cur_id[s] = mid[static_cast<uint32_t>(s) * 32u + lane];
+      }
+      __syncwarp();
+      if (++iter == a.reset_iter) {
+        hash_clear(hash, a.hash_slots);
+        __syncwarp();
+#pragma unroll
+        for (int s = 0; s < KM_S; s++) hash_insert(hash, hmask, cur_id[s] & kMaskedTomb);
+        __syncwarp();
+        iter = 0;
+      }
+    }
+    if (!ok) break;
+    it_all += (lane == 0) ? total : 0u;
+    uint64_t k2[EF];
+    uint32_t i2[EF];
+#pragma unroll
+    for (int s = 0; s < EF; s++) {
+      k2[s] = s < KM_S ? top_key[s < KM_S ? s : 0] : (s == KM_S ? cand_key : ~0ull);
+      i2[s] = s < KM_S ? top_id[s < KM_S ? s : 0] : (s == KM_S ? cand_id : kTomb);
+    }
+    warp_sort_kv<EF>(k2, i2);
+    uint32_t* orow = a.out + static_cast<uint64_t>(qid) * a.out_width;
+#pragma unroll
+    for (int s = 0; s < EF; s++) {
+      const uint32_t pos = static_cast<uint32_t>(s) * 32u + lane;
+      if (pos < KM + 32u && pos < a.out_width) orow[pos] = i2[s] & kMaskedTomb;
+    }
+  }
+  if (!ok) {
+    if (lane == 0) raise_error(a.status, kErrWait);
+    mbar_wait_bounded(mbar, phase ^ 1u);
+  }
+  if (lane == 0) {
+    if (ev) atomicAdd(a.evals, ev);
+    if (it_all) atomicAdd(a.iters, it_all);
+  }
+}
+
+size_t search_mk_smem(uint32_t d, uint32_t hash_slots, uint32_t rows, uint32_t km) {
+  return 16 + 12 * static_cast<size_t>(km) + 4 * static_cast<size_t>(hash_slots) +
+         static_cast<size_t>(rows) * 4 * d;
+}
+
+template <int KM_S, int KS>
+static cudaError_t launch_search_mk(const SearchArgs& a, int num_sms, size_t smem_optin,
+                                    cudaStream_t st) {
+  constexpr int ROWS = 8;
+  const size_t smem = search_mk_smem(a.d, a.hash_slots, ROWS, 32u * KM_S);
+  if (smem > smem_optin) return cudaErrorInvalidValue;
+  auto kern = k_search_mk<KM_S, KS, ROWS>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem);
+  if (e != cudaSuccess) return e;
+  if (a.max_blocks_per_sm && per_sm > static_cast<int>(a.max_blocks_per_sm))
+    per_sm = static_cast<int>(a.max_blocks_per_sm);
+  if (per_sm < 1) per_sm = 1;
+  uint64_t blocks = static_cast<uint64_t>(num_sms) * per_sm;
+  const uint64_t nq = a.queries ? a.nq : a.n;
+  if (blocks > nq) blocks = nq;
+  kern<<<static_cast<unsigned>(blocks), 32, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 size_t search_m32_smem(uint32_t d, uint32_t hash_slots, uint32_t rows) {
   return 16 + 256 + 128 + 4 * static_cast<size_t>(hash_slots) + static_cast<size_t>(rows) * 4 * d;
 }
@@ -698,32 +727,6 @@ bool search_supported(uint32_t d, uint32_t km, uint32_t kp, uint32_t kd) {
          km <= 96 && (km % 32) == 0;
 }
 
-size_t search_smem_per_warp(uint32_t d, uint32_t hash_slots) {
-  return 16 + 4 * static_cast<size_t>(hash_slots) + 32 * 4 * static_cast<size_t>(d);
-}
-
-template <int KM_S, int KS>
-static cudaError_t launch_search_t(const SearchArgs& a, int num_sms, size_t smem_optin,
-                                   cudaStream_t st) {
-  const size_t smem = search_smem_per_warp(a.d, a.hash_slots);
-  if (smem > smem_optin) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(k_search<KM_S, KS>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem));
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<KM_S, KS>, 32, smem);
-  if (e != cudaSuccess) return e;
-  if (a.max_blocks_per_sm && per_sm > static_cast<int>(a.max_blocks_per_sm))
-    per_sm = static_cast<int>(a.max_blocks_per_sm);
-  if (per_sm < 1) per_sm = 1;
-  uint64_t blocks = static_cast<uint64_t>(num_sms) * per_sm;
-  const uint64_t nq = a.queries ? a.nq : a.n;
-  if (blocks > nq) blocks = nq;
-  k_search<KM_S, KS><<<static_cast<unsigned>(blocks), 32, smem, st>>>(a);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, cudaStream_t st) {
   if (!search_supported(a.d, a.km, a.kp, a.kd)) return cudaErrorInvalidValue;
   const int km_s = static_cast<int>(a.km / 32);
@@ -741,11 +744,13 @@ cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, c
       return r16 ? launch_search_m32<16, 16>(a, num_sms, smem_optin, st)
                  : launch_search_m32<16, 8>(a, num_sms, smem_optin, st);
     case 2:
-      return small ? launch_search_t<2, 8>(a, num_sms, smem_optin, st)
-                   : launch_search_t<2, 16>(a, num_sms, smem_optin, st);
+      if (a.d <= 224) return launch_search_mk<2, 7>(a, num_sms, smem_optin, st);
+      return small ? launch_search_mk<2, 8>(a, num_sms, smem_optin, st)
+                   : launch_search_mk<2, 16>(a, num_sms, smem_optin, st);
     default:
-      return small ? launch_search_t<3, 8>(a, num_sms, smem_optin, st)
-                   : launch_search_t<3, 16>(a, num_sms, smem_optin, st);
+      if (a.d <= 224) return launch_search_mk<3, 7>(a, num_sms, smem_optin, st);
+      return small ? launch_search_mk<3, 8>(a, num_sms, smem_optin, st)
+                   : launch_search_mk<3, 16>(a, num_sms, smem_optin, st);
   }
 }
 

@@ -75,7 +75,8 @@ def make_dataset(n: int, d: int, q: int | None = None, gt_k: int = 128, seed: in
 def make_dataset_cuda(n: int, d: int, q: int | None = None, gt_k: int = 128, centers: int = 64,
                       sigma: float = 0.3, query_scale: float = 0.6, shift_norm: float = 2.0,
                       noise: float = 0.2, cosine: bool = False, seed: int = 1234,
-                      chunk: int = 4096, device: str = "cuda", return_queries: bool = False):
+                      chunk: int = 4096, device: str = "cuda", return_queries: bool = False,
+                      with_gt: bool = True):
     """The same recipe on the GPU with torch (for N in the millions).  Returns device tensors
     (base float32 N x D, gt int32 viewed as uint32 Q x gt_k[, queries float32 Q x D])."""
     import torch
@@ -99,6 +100,8 @@ def make_dataset_cuda(n: int, d: int, q: int | None = None, gt_k: int = 128, cen
     if cosine:
         base = base / base.norm(dim=1, keepdim=True)
         queries = queries / queries.norm(dim=1, keepdim=True)
+    if not with_gt:  # the caller computes the ground truth (e.g. pg_ground_truth)
+        return base.contiguous(), None, queries.contiguous()
     prev = torch.backends.cuda.matmul.allow_tf32
     torch.backends.cuda.matmul.allow_tf32 = False
     try:
