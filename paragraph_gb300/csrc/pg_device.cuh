@@ -29,7 +29,7 @@ __device__ __forceinline__ float dist_seq(const float* __restrict__ x, const flo
     const float4* a = reinterpret_cast<const float4*>(x);
     const float4* b = reinterpret_cast<const float4*>(y);
     const uint32_t n4 = d >> 2;
-#pragma unroll 5
+#pragma unroll 10
     for (uint32_t i = 0; i < n4; i++) {
       float4 u = __ldg(a + i);
       float4 v = __ldg(b + i);

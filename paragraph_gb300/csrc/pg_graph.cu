@@ -99,7 +99,9 @@ __device__ __forceinline__ void dist_seq_multi(const float* __restrict__ brow,
   }
   const float4* b4 = reinterpret_cast<const float4*>(brow);
   const uint32_t n4 = d >> 2;
-#pragma unroll 2
+  // four steps per pass keep (1 + E) * 4 row loads in flight: the rows come from L2, and the
+  // chain's order leaves no other parallelism
+#pragma unroll 4
   for (uint32_t i = 0; i < n4; i++) {
     const float4 u = __ldg(b4 + i);
 #pragma unroll
