@@ -91,17 +91,6 @@ __device__ __forceinline__ uint32_t hslot(uint32_t key, uint32_t mask) {
   return h & mask;
 }
 
-__device__ __forceinline__ bool hash_contains(const uint32_t* t, uint32_t mask, uint32_t key) {
-  uint32_t s = hslot(key, mask);
-  for (uint32_t probe = 0; probe <= mask; probe++) {
-    const uint32_t v = t[s];
-    if (v == 0) return false;
-    if (v == key + 1) return true;
-    s = (s + 1) & mask;
-  }
-  return false;
-}
-
 __device__ __forceinline__ void hash_insert(uint32_t* t, uint32_t mask, uint32_t key) {
   uint32_t s = hslot(key, mask);
   for (uint32_t probe = 0; probe <= mask; probe++) {
@@ -109,6 +98,20 @@ __device__ __forceinline__ void hash_insert(uint32_t* t, uint32_t mask, uint32_t
     if (old == 0 || old == key + 1) return;
     s = (s + 1) & mask;
   }
+}
+
+// Inserts key unless present, in one probe sequence; true when it was absent
+// (warp_level_test_and_set, Ghashtable.cuh:39-64).  The lanes of a warp insert distinct keys, so
+// a concurrent claim of a slot by another lane only moves the probe on.
+__device__ __forceinline__ bool hash_test_and_set(uint32_t* t, uint32_t mask, uint32_t key) {
+  uint32_t s = hslot(key, mask);
+  for (uint32_t probe = 0; probe <= mask; probe++) {
+    const uint32_t old = atomicCAS(t + s, 0u, key + 1);
+    if (old == 0) return true;
+    if (old == key + 1) return false;
+    s = (s + 1) & mask;
+  }
+  return false;  // cannot happen: the table has twice the slots of the ids it ever holds
 }
 
 __device__ __forceinline__ void hash_clear(uint32_t* t, uint32_t slots) {
@@ -360,9 +363,7 @@ __global__ void __launch_bounds__(32, KSTEPS <= 8 ? 20 : 12) k_search_m32(Search
       const bool valid = node != kTomb;
       const unsigned same = __match_any_sync(kFull, node);
       const bool first = lane == static_cast<uint32_t>(__ffs(static_cast<int>(same)) - 1);
-      const bool newc = valid && first && !hash_contains(hash, hmask, node);
-      __syncwarp();
-      if (newc) hash_insert(hash, hmask, node);
+      const bool newc = valid && first && hash_test_and_set(hash, hmask, node);
       __syncwarp();
       const float dist = score_passes<KSTEPS, ROWS>(a, q, node, newc, rows, mbar, phase, ok);
       if (!ok) break;
@@ -577,9 +578,7 @@ __global__ void __launch_bounds__(32, KSTEPS <= 8 ? 16 : 8) k_search_mk(SearchAr
       const bool valid = node != kTomb;
       const unsigned same = __match_any_sync(kFull, node);
       const bool first = lane == static_cast<uint32_t>(__ffs(static_cast<int>(same)) - 1);
-      const bool newc = valid && first && !hash_contains(hash, hmask, node);
-      __syncwarp();
-      if (newc) hash_insert(hash, hmask, node);
+      const bool newc = valid && first && hash_test_and_set(hash, hmask, node);
       __syncwarp();
       const float dist = score_passes<KSTEPS, ROWS>(a, q, node, newc, rows, mbar, phase, ok);
       if (!ok) break;
