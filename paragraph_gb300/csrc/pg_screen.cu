@@ -1,7 +1,7 @@
 // pg_screen.cu -- screened prune + reverse (K6/K10) with a BF16 tensor-core Gram.
 //
 // Same result as k_prune_reverse (strict rounds), bit for bit.  Per node (one warp, up to 64
-// candidates):
+// candidates; up to 96 in the three-slot variant, whose Gram is built in two passes):
 //   1. one pass over the candidate rows: each lane runs the exact FP32 chain dist(b, c) for its
 //      candidates (distance_between's order, Gbuilder.cuh:785-797) and, from the same loads,
 //      rounds the row to BF16 and accumulates two norms per row, |x| and |x - bf16(x)|;
@@ -26,8 +26,6 @@
 namespace pg {
 
 namespace {
-
-constexpr int kScrC = 64;  // candidates per node handled by the screened kernel
 
 __device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi, float& elo, float& ehi) {
   const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
@@ -72,12 +70,17 @@ __host__ __device__ inline uint32_t screen_dp(uint32_t d) { return (d + 15u) / 1
 namespace {
 
 constexpr uint32_t kChunkStride = 24;  // BF16 per chunk row: 48 B keeps ldmatrix rows conflict-free
-constexpr uint32_t kTri = kScrC * (kScrC - 1) / 2;  // packed strictly-lower Gram entries
+
+template <int NS>
+struct ScreenShape {
+  static constexpr uint32_t kC = 32u * NS;                 // candidates per node
+  static constexpr uint32_t kTri = kC * (kC - 1) / 2;      // packed strictly-lower Gram entries
+};
 
 // Per-warp shared memory of the screened kernels.
 struct ScreenSmem {
-  __nv_bfloat16* chunk;  // kScrC x kChunkStride: one K chunk of the BF16 rows
-  float* G;              // kTri: packed strictly-lower Gram
+  __nv_bfloat16* chunk;  // C x kChunkStride: one K chunk of the BF16 rows
+  float* G;              // C(C-1)/2: packed strictly-lower Gram
   uint32_t* ids;         // sorted ids
   float* dist;           // sorted exact distances to the node
   float* nrm;            // |x| per original slot
@@ -87,17 +90,19 @@ struct ScreenSmem {
   uint32_t* kept_i;      // kept entries: id
 };
 
+template <int NS>
 __device__ __forceinline__ ScreenSmem screen_smem(unsigned char* raw) {
+  constexpr uint32_t C = ScreenShape<NS>::kC;
   ScreenSmem m;
   m.chunk = reinterpret_cast<__nv_bfloat16*>(raw);
-  m.G = reinterpret_cast<float*>(raw + static_cast<size_t>(kScrC) * kChunkStride * 2);
-  m.ids = reinterpret_cast<uint32_t*>(m.G + kTri);
-  m.dist = reinterpret_cast<float*>(m.ids + kScrC);
-  m.nrm = m.dist + kScrC;
-  m.err = m.nrm + kScrC;
-  m.orig = reinterpret_cast<uint32_t*>(m.err + kScrC);
-  m.kept_o = m.orig + kScrC;
-  m.kept_i = m.kept_o + kScrC;
+  m.G = reinterpret_cast<float*>(raw + static_cast<size_t>(C) * kChunkStride * 2);
+  m.ids = reinterpret_cast<uint32_t*>(m.G + ScreenShape<NS>::kTri);
+  m.dist = reinterpret_cast<float*>(m.ids + C);
+  m.nrm = m.dist + C;
+  m.err = m.nrm + C;
+  m.orig = reinterpret_cast<uint32_t*>(m.err + C);
+  m.kept_o = m.orig + C;
+  m.kept_i = m.kept_o + C;
   return m;
 }
 
@@ -105,27 +110,32 @@ __device__ __forceinline__ uint32_t tri_index(uint32_t r, uint32_t c) {  // r > 
   return r * (r - 1) / 2 + c;
 }
 
-// Steps 1 and 2 for one node: exact chains dist(b, id[s]) (FLT_MAX where !valid[s]), BF16
-// rounding, norms, and the streamed tensor-core Gram of the 64 slots into sm.G / sm.nrm / sm.err.
-// Lane l owns slots l and 32 + l.
-__device__ __forceinline__ void screen_rows_and_gram(const float* __restrict__ base, uint32_t d,
-                                                     const float* __restrict__ brow,
-                                                     const uint32_t (&id)[2],
-                                                     const bool (&valid)[2], const ScreenSmem& sm,
-                                                     float (&dist)[2]) {
+// One streamed pass over the candidate rows, 16-wide K chunks through sm.chunk, accumulating the
+// lower-triangle m16n8 Gram tiles of row blocks [MT_LO, MT_HI) (row block mt covers column tiles
+// 0 .. 2 mt + 1) in registers and storing them packed into sm.G.  The FIRST pass also runs the
+// exact chains dist(b, id[s]) (FLT_MAX where !valid[s]) and the two norms per row.  Lane l owns
+// slots l, 32 + l, ...
+template <int NS, int MT_LO, int MT_HI, bool FIRST>
+__device__ __forceinline__ void screen_pass(const float* __restrict__ base, uint32_t d,
+                                            const float* __restrict__ brow,
+                                            const uint32_t (&id)[NS], const bool (&valid)[NS],
+                                            const ScreenSmem& sm, float (&dist)[NS]) {
+  constexpr int kTiles = (MT_HI * (MT_HI + 1)) - (MT_LO * (MT_LO + 1));  // sum of 2 mt + 2
   const uint32_t lane = lane_id();
   const uint32_t dp = screen_dp(d);
   const uint32_t g = lane >> 2, t4 = lane & 3u;
   const float4* b4 = reinterpret_cast<const float4*>(brow);
-  const float4* r4[2];
+  const float4* r4[NS];
 #pragma unroll
-  for (int s = 0; s < 2; s++)
+  for (int s = 0; s < NS; s++)
     r4[s] = reinterpret_cast<const float4*>(valid[s] ? base + static_cast<uint64_t>(id[s]) * d
                                                      : brow);
-  float acc[2] = {0.f, 0.f}, nn[2] = {0.f, 0.f}, ee[2] = {0.f, 0.f};
-  float gm[20][4];  // lower-triangle m16n8 tiles: tile (mt, nt) at mt*(mt+1) + nt, nt <= 2mt+1
+  float acc[NS], nn[NS], ee[NS];
 #pragma unroll
-  for (int i = 0; i < 20; i++)
+  for (int s = 0; s < NS; s++) acc[s] = nn[s] = ee[s] = 0.f;
+  float gm[kTiles][4];  // tile (mt, nt) at mt*(mt+1) - MT_LO*(MT_LO+1) + nt
+#pragma unroll
+  for (int i = 0; i < kTiles; i++)
 #pragma unroll
     for (int j = 0; j < 4; j++) gm[i][j] = 0.f;
   const uint32_t n4 = d >> 2;
@@ -134,21 +144,24 @@ __device__ __forceinline__ void screen_rows_and_gram(const float* __restrict__ b
     for (uint32_t q = 0; q < 4; q++) {
       const uint32_t i = (k0 >> 2) + q;  // float4 index
       const bool in = i < n4;
-      const float4 u = in ? __ldg(b4 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (FIRST && in) u = __ldg(b4 + i);
 #pragma unroll
-      for (int s = 0; s < 2; s++) {
+      for (int s = 0; s < NS; s++) {
         const float4 v = in ? __ldg(r4[s] + i) : make_float4(0.f, 0.f, 0.f, 0.f);
         uint2 packed = make_uint2(0u, 0u);
         if (in) {
-          acc[s] = fmaf(u.x, v.x, acc[s]);
-          acc[s] = fmaf(u.y, v.y, acc[s]);
-          acc[s] = fmaf(u.z, v.z, acc[s]);
-          acc[s] = fmaf(u.w, v.w, acc[s]);
           float e0, e1, e2, e3;
           packed.x = bf16x2_bits(v.x, v.y, e0, e1);
           packed.y = bf16x2_bits(v.z, v.w, e2, e3);
-          nn[s] = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, nn[s]))));
-          ee[s] = fmaf(e0, e0, fmaf(e1, e1, fmaf(e2, e2, fmaf(e3, e3, ee[s]))));
+          if (FIRST) {
+            acc[s] = fmaf(u.x, v.x, acc[s]);
+            acc[s] = fmaf(u.y, v.y, acc[s]);
+            acc[s] = fmaf(u.z, v.z, acc[s]);
+            acc[s] = fmaf(u.w, v.w, acc[s]);
+            nn[s] = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, nn[s]))));
+            ee[s] = fmaf(e0, e0, fmaf(e1, e1, fmaf(e2, e2, fmaf(e3, e3, ee[s]))));
+          }
         }
         const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
         *reinterpret_cast<uint2*>(sm.chunk + j * kChunkStride + 4 * q) =
@@ -157,51 +170,73 @@ __device__ __forceinline__ void screen_rows_and_gram(const float* __restrict__ b
     }
     __syncwarp();
 #pragma unroll
-    for (int mt = 0; mt < 4; mt++) {
+    for (int mt = MT_LO; mt < MT_HI; mt++) {
       uint32_t af[4];
       ldsm_x4(af, sm.chunk + (16 * mt + (lane & 15u)) * kChunkStride + (lane >> 4) * 8);
 #pragma unroll
       for (int nt = 0; nt <= 2 * mt + 1; nt++) {
         uint32_t bf[2];
         ldsm_x2(bf, sm.chunk + (8 * nt + (lane & 7u)) * kChunkStride + ((lane >> 3) & 1u) * 8);
-        mma_bf16(gm[mt * (mt + 1) + nt], af, bf);
+        mma_bf16(gm[mt * (mt + 1) - MT_LO * (MT_LO + 1) + nt], af, bf);
       }
     }
     __syncwarp();
   }
 #pragma unroll
-  for (int mt = 0; mt < 4; mt++)
+  for (int mt = MT_LO; mt < MT_HI; mt++)
 #pragma unroll
     for (int nt = 0; nt <= 2 * mt + 1; nt++) {
-      const float* c = gm[mt * (mt + 1) + nt];
+      const float* c = gm[mt * (mt + 1) - MT_LO * (MT_LO + 1) + nt];
       const uint32_t r0 = 16 * mt + g, c0 = 8 * nt + 2 * t4;
       if (r0 > c0) sm.G[tri_index(r0, c0)] = c[0];
       if (r0 > c0 + 1) sm.G[tri_index(r0, c0 + 1)] = c[1];
       if (r0 + 8 > c0) sm.G[tri_index(r0 + 8, c0)] = c[2];
       if (r0 + 8 > c0 + 1) sm.G[tri_index(r0 + 8, c0 + 1)] = c[3];
     }
+  if (FIRST) {
 #pragma unroll
-  for (int s = 0; s < 2; s++) {
-    const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
-    sm.nrm[j] = valid[s] ? sqrtf(nn[s]) * 1.0001f : 0.f;
-    sm.err[j] = valid[s] ? sqrtf(ee[s]) * 1.0001f : 0.f;
-    dist[s] = valid[s] ? -acc[s] : FLT_MAX;
+    for (int s = 0; s < NS; s++) {
+      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+      sm.nrm[j] = valid[s] ? sqrtf(nn[s]) * 1.0001f : 0.f;
+      sm.err[j] = valid[s] ? sqrtf(ee[s]) * 1.0001f : 0.f;
+      dist[s] = valid[s] ? -acc[s] : FLT_MAX;
+    }
   }
 }
 
-// Sorts the 64 slots by (exact distance, slot) into sm.ids / sm.dist / sm.orig (first c).
-__device__ __forceinline__ void screen_sort(uint32_t (&id)[2], const float (&dist)[2], uint32_t c,
-                                            const ScreenSmem& sm) {
-  const uint32_t lane = lane_id();
-  uint64_t key[2];
-#pragma unroll
-  for (int s = 0; s < 2; s++) {
-    const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
-    key[s] = (j < c) ? pack_key(dist[s], j) : ~0ull;
+// Steps 1 and 2: exact chains, norms and the whole lower-triangle Gram of the 32 NS slots (two
+// register passes for 96 candidates: row blocks 0-3, then 4-5).
+template <int NS>
+__device__ __forceinline__ void screen_rows_and_gram(const float* __restrict__ base, uint32_t d,
+                                                     const float* __restrict__ brow,
+                                                     const uint32_t (&id)[NS],
+                                                     const bool (&valid)[NS],
+                                                     const ScreenSmem& sm, float (&dist)[NS]) {
+  if constexpr (NS == 2) {
+    screen_pass<2, 0, 4, true>(base, d, brow, id, valid, sm, dist);
+  } else {
+    screen_pass<3, 0, 4, true>(base, d, brow, id, valid, sm, dist);
+    screen_pass<3, 4, 6, false>(base, d, brow, id, valid, sm, dist);
   }
-  warp_sort_kv<2>(key, id);
+}
+
+// Sorts the slots by (exact distance, slot) into sm.ids / sm.dist / sm.orig (first c).
+template <int NS>
+__device__ __forceinline__ void screen_sort(const uint32_t (&idin)[NS], const float (&dist)[NS],
+                                            uint32_t c, const ScreenSmem& sm) {
+  constexpr int E = NS <= 2 ? 2 : 4;  // the bitonic network wants a power of two
+  const uint32_t lane = lane_id();
+  uint64_t key[E];
+  uint32_t id[E];
 #pragma unroll
-  for (int s = 0; s < 2; s++) {
+  for (int s = 0; s < E; s++) {
+    const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+    key[s] = (s < NS && j < c) ? pack_key(dist[s < NS ? s : 0], j) : ~0ull;
+    id[s] = s < NS ? idin[s < NS ? s : 0] : kTomb;
+  }
+  warp_sort_kv<E>(key, id);
+#pragma unroll
+  for (int s = 0; s < E; s++) {
     const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
     if (i < c) {
       sm.ids[i] = id[s];
@@ -262,29 +297,34 @@ __device__ __forceinline__ bool screen_occluded(const float* __restrict__ base, 
 }  // namespace
 
 // bytes of shared memory per warp
-size_t screen_smem_per_warp(uint32_t /*d*/) {
-  return static_cast<size_t>(kScrC) * kChunkStride * 2  // one K chunk of the BF16 rows
-         + static_cast<size_t>(kTri) * 4                 // G, strictly lower triangle
-         + static_cast<size_t>(kScrC) * 4 * 7;           // ids, dist, |x|, |e|, slot, kept x2
+template <int NS>
+size_t screen_smem_ns() {
+  constexpr size_t C = ScreenShape<NS>::kC;
+  return C * kChunkStride * 2                          // one K chunk of the BF16 rows
+         + static_cast<size_t>(ScreenShape<NS>::kTri) * 4  // G, strictly lower triangle
+         + C * 4 * 7;                                  // ids, dist, |x|, |e|, slot, kept x2
 }
+
+size_t screen_smem_per_warp(uint32_t /*d*/) { return screen_smem_ns<2>(); }
 
 bool screen_supported(uint32_t c, uint32_t d, int strict) {
-  return strict && c <= static_cast<uint32_t>(kScrC) && d >= 4 && d <= 1024 && (d % 4) == 0;
+  return strict && c <= ScreenShape<3>::kC && d >= 4 && d <= 1024 && (d % 4) == 0;
 }
 
-__global__ void __launch_bounds__(32, 16) k_prune_screen(PruneArgs a) {
+template <int NS>
+__global__ void __launch_bounds__(32, NS == 2 ? 16 : 8) k_prune_screen(PruneArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const ScreenSmem sm = screen_smem(smem_raw);
+  const ScreenSmem sm = screen_smem<NS>(smem_raw);
   const uint32_t lane = lane_id();
   const uint32_t d = a.d;
   const float c_acc = static_cast<float>(screen_dp(d) + 32) * 4.76837158e-07f;  // 2^-21
   const float c_seq = static_cast<float>(d + 2) * 1.19209290e-07f;              // 2^-23
   uint64_t ev = 0, resc = 0;
   for (uint64_t b = blockIdx.x; b < a.n; b += gridDim.x) {
-    uint32_t id[2];
-    bool valid[2];
+    uint32_t id[NS];
+    bool valid[NS];
 #pragma unroll
-    for (int s = 0; s < 2; s++) {
+    for (int s = 0; s < NS; s++) {
       const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
       uint32_t x = (j < a.c) ? a.graph[b * a.c + j] : kTomb;
       if (x >= a.n && x != kTomb && x != kMaskedTomb) {
@@ -294,12 +334,13 @@ __global__ void __launch_bounds__(32, 16) k_prune_screen(PruneArgs a) {
       id[s] = x;
       valid[s] = (x != kTomb && x != static_cast<uint32_t>(b) && x != kMaskedTomb);
     }
-    float dist[2];
-    screen_rows_and_gram(a.base, d, a.base + b * d, id, valid, sm, dist);
-    const unsigned v0 = __ballot_sync(kFull, valid[0]);  // every lane takes part
-    const unsigned v1 = __ballot_sync(kFull, valid[1]);
-    ev += (lane == 0) ? (__popc(v0) + __popc(v1)) : 0u;
-    screen_sort(id, dist, a.c, sm);
+    float dist[NS];
+    screen_rows_and_gram<NS>(a.base, d, a.base + b * d, id, valid, sm, dist);
+    uint32_t nv = 0;
+#pragma unroll
+    for (int s = 0; s < NS; s++) nv += __popc(__ballot_sync(kFull, valid[s]));  // all lanes
+    ev += (lane == 0) ? nv : 0u;
+    screen_sort<NS>(id, dist, a.c, sm);
 
     const uint32_t first = sm.ids[0];
     if (first == kTomb || first == kMaskedTomb) {
@@ -345,9 +386,8 @@ __global__ void __launch_bounds__(32, 16) k_prune_screen(PruneArgs a) {
 
 template <typename Args>
 static cudaError_t launch_screen_kernel(void (*kern)(Args), const Args& a, uint64_t n,
-                                        uint32_t d, uint32_t carveout, int num_sms,
+                                        size_t smem, uint32_t carveout, int num_sms,
                                         size_t smem_optin, cudaStream_t st) {
-  const size_t smem = screen_smem_per_warp(d);
   if (smem > smem_optin) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
@@ -375,7 +415,11 @@ cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_opt
                                 cudaStream_t st) {
   if (!screen_supported(a.c, a.d, a.strict)) return cudaErrorInvalidValue;
   if (a.carveout > 100) return cudaErrorInvalidValue;
-  return launch_screen_kernel(k_prune_screen, a, a.n, a.d, a.carveout, num_sms, smem_optin, st);
+  if (a.c <= ScreenShape<2>::kC)
+    return launch_screen_kernel(k_prune_screen<2>, a, a.n, screen_smem_ns<2>(), a.carveout,
+                                num_sms, smem_optin, st);
+  return launch_screen_kernel(k_prune_screen<3>, a, a.n, screen_smem_ns<3>(), a.carveout,
+                              num_sms, smem_optin, st);
 }
 
 }  // namespace pg

@@ -255,3 +255,27 @@ def test_screened_build_with_hubs_and_duplicates(pg, handle, golden_dir):
     f = load(golden_dir, "edge")
     g, p, st, ref = _build_both(pg, handle, f["base"], f["gt"], screen=pg.SCREEN_BF16)
     assert np.array_equal(g, ref["graph"])
+
+
+@pytest.mark.parametrize("n,d,degree,seed,cosine", [(8000, 512, 48, 5, True),
+                                                    (6000, 200, 32, 6, False)])
+def test_screened_build_96_candidates(pg, handle, n, d, degree, seed, cosine):
+    """L = 96: the screened prune's three-slot variant (96 candidates, Gram in two passes)."""
+    from paragraph_gb300 import datagen
+    base, q = datagen.make_base_queries(n, d, seed=seed, cosine=cosine)
+    gt = datagen.ground_truth(base, q, 128)
+    g, p, st, ref = _build_both(pg, handle, base, gt, degree=degree, beam=96,
+                                screen=pg.SCREEN_BF16)
+    assert np.array_equal(p, ref["proj"])
+    bad = (g != ref["graph"]).any(axis=1)
+    assert not bad.any(), f"{bad.sum()} rows differ"
+    assert st.evals_total == ref["stats"]["evals_total"]
+    assert sum(st.rescored) < 0.5 * sum(st.evals_prune)
+
+
+def test_screened_96_with_hubs_and_duplicates(pg, handle, golden_dir):
+    f = load(golden_dir, "edge")
+    g, p, st, ref = _build_both(pg, handle, f["base"], f["gt"], degree=32, beam=96,
+                                screen=pg.SCREEN_BF16)
+    assert np.array_equal(g, ref["graph"])
+    assert st.evals_total == ref["stats"]["evals_total"]
