@@ -31,8 +31,16 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "distance_evals_per_s (build, 1Mx200 IP, M=32, L=64, screened vs FP32, identical edges)"
 UNIT = "evals/s"
+
+
+def metric_name(args) -> str:
+    """The metric string of the workload the arguments describe (the 1M x 200 inner-product,
+    M = 32, L = 64 build by default)."""
+    n = "1M" if args.n == 1_000_000 else str(args.n)
+    kind = "cosine" if args.cosine else "IP"
+    return (f"distance_evals_per_s (build, {n}x{args.d} {kind}, M={args.degree}, L={args.beam}, "
+            "screened vs FP32, identical edges)")
 
 
 def parse():
@@ -50,7 +58,7 @@ def parse():
                     help="target length of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--screen", default="bf16", choices=["bf16", "none"],
+    ap.add_argument("--screen", default="fp16", choices=["fp16", "bf16", "none"],
                     help="path timed for `value`; the other one is timed beside it")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the other path")
     ap.add_argument("--no-index", action="store_true",
@@ -186,7 +194,8 @@ def search_roofline(st, args, peak_gbs, peak_kind, rounds):
         for line in open(tpath):
             if line.startswith("search_dram_bytes_per_launch:"):
                 traffic = int(line.split(":")[1])
-    return {"kernel": "k_search_m32 (K4/K8 beam search)", "bound": "hbm",
+    kname = "k_search_m32" if args.beam <= 32 * 2 else "k_search_mk"
+    return {"kernel": f"{kname} (K4/K8 beam search)", "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak_gbs, "peak_kind": peak_kind,
             "unit": "GB/s", "frac": round(achieved / peak_gbs, 4),
             "traffic": traffic, "algorithmic_bytes_per_launch": round(tot_bytes / rounds),
@@ -255,7 +264,7 @@ def run_reference(args):
         if i >= args.warmup:
             vals.append(v)
     value = statistics.mean(vals)
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+    line = {"metric": metric_name(args), "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": steps, "warmup": args.warmup, "ms_per_step": None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded mixture-of-Gaussians stand-in for T2I-style data)",
@@ -283,7 +292,7 @@ def run_ours(args):
     base, gt = wl[0], wl[1]
     queries = wl[2] if want_q else None
     torch.cuda.synchronize()
-    screen = pg.SCREEN_BF16 if args.screen == "bf16" else pg.SCREEN_NONE
+    screen = {"bf16": pg.SCREEN_BF16, "fp16": pg.SCREEN_FP16, "none": pg.SCREEN_NONE}[args.screen]
     params = pg.default_params(args.degree, args.beam, screen=screen)
     other = pg.default_params(args.degree, args.beam,
                               screen=pg.SCREEN_NONE if screen else pg.SCREEN_BF16)
@@ -430,10 +439,10 @@ def run_ours(args):
             index_line["cpu_oracle_cores"] = threads
     s = stats[-1]
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        line = {"metric": metric_name(args), "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32" if args.screen == "none" else "f32+bf16",
+                "dtype": "f32" if args.screen == "none" else "f32+" + args.screen,
                 "data": "synthetic (seeded mixture-of-Gaussians stand-in for T2I-style data)",
                 "config": {"workload": f"ParaGraph build {args.n}x{args.d} IP, gt top-128, "
                                        f"M={args.degree}, L={args.beam}",
@@ -501,7 +510,7 @@ def run_batched(args):
         del b, q
     torch.cuda.empty_cache()
     gen_s = time.perf_counter() - t0
-    screen = pg.SCREEN_BF16 if args.screen == "bf16" else pg.SCREEN_NONE
+    screen = {"bf16": pg.SCREEN_BF16, "fp16": pg.SCREEN_FP16, "none": pg.SCREEN_NONE}[args.screen]
     params = pg.default_params(args.degree, args.beam, screen=screen, flags=pg.FLAG_CUDA_GRAPH)
     tuning = None
     if args.autotune:
@@ -536,10 +545,10 @@ def run_batched(args):
     torch.cuda.synchronize()
     ms_alone = a.elapsed_time(b_)
     identical = bool(torch.equal(graph, alone))
-    line = {"metric": METRIC + " -- batched form", "value": st.evals_total / (ms / 1e3),
+    line = {"metric": metric_name(args) + " -- batched form", "value": st.evals_total / (ms / 1e3),
             "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32" if args.screen == "none" else "f32+bf16",
+            "vs_baseline": None, "dtype": "f32" if args.screen == "none" else "f32+" + args.screen,
             "data": "synthetic (seeded mixture-of-Gaussians, one set per sub-index)",
             "config": {"workload": f"{args.batched} sub-indexes, sizes log-uniform in "
                                    f"[{args.min_points}, {args.max_points}] (total {total}), "

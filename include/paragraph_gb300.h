@@ -42,7 +42,10 @@ typedef enum pg_status {
 typedef enum pg_screen {
   PG_SCREEN_NONE = 0, /* plain FP32: every distance in the reference's own FP32 order */
   PG_SCREEN_BF16 = 1, /* BF16 tensor-core screening + exact FP32 re-scoring inside a margin */
-  PG_SCREEN_FP8 = 2   /* FP8 E4M3 per-vector-scaled screening + exact FP32 re-scoring */
+  PG_SCREEN_FP8 = 2,  /* FP8 E4M3 per-vector-scaled screening (not built: see the error study) */
+  PG_SCREEN_FP16 = 3  /* FP16 tensor-core screening (11-bit significands: a margin about 8x
+                         tighter than BF16's) + exact FP32 re-scoring; values beyond FP16's range
+                         only make every test of their node exact */
 } pg_screen;
 
 /* Build parameters.  pg_params_default() maps (M, L) onto the reference driver's constants

@@ -24,7 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 TOMB = 0xFFFFFFFF
 
 PG_OK, PG_EINVAL, PG_ECUDA, PG_ENOMEM, PG_ETIMEOUT, PG_EUNSUPPORTED, PG_EIO = range(7)
-SCREEN_NONE, SCREEN_BF16, SCREEN_FP8 = 0, 1, 2
+SCREEN_NONE, SCREEN_BF16, SCREEN_FP8, SCREEN_FP16 = 0, 1, 2, 3
 FLAG_VALIDATE_INPUT = 1
 FLAG_CUDA_GRAPH = 2
 

@@ -232,8 +232,9 @@ int check_params(const pg_params* p, uint64_t n, uint32_t d, uint64_t q) {
     if (p->kd > p->proj_degree || p->kd > p->degree)
       return fail(PG_EINVAL, "kd=%u exceeds a graph degree", p->kd);
   }
-  if (p->screen != PG_SCREEN_NONE && p->screen != PG_SCREEN_BF16)
-    return fail(PG_EUNSUPPORTED, "screen=%u: only PG_SCREEN_NONE and PG_SCREEN_BF16 are built",
+  if (p->screen != PG_SCREEN_NONE && p->screen != PG_SCREEN_BF16 && p->screen != PG_SCREEN_FP16)
+    return fail(PG_EUNSUPPORTED,
+                "screen=%u: PG_SCREEN_NONE, PG_SCREEN_BF16 and PG_SCREEN_FP16 are built",
                 p->screen);
   return PG_OK;
 }
@@ -398,7 +399,8 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
       pr.status = h->d_status;
       pr.rescored = cnt + C_RESCORED + r;
       pr.carveout = h->tune.screen_carveout;
-      if (p->screen == PG_SCREEN_BF16 && pg::screen_supported(pr.c, d, pr.strict))
+      pr.screen_half = p->screen == PG_SCREEN_FP16;
+      if (p->screen != PG_SCREEN_NONE && pg::screen_supported(pr.c, d, pr.strict))
         PG_CUDA(pg::launch_prune_screen(pr, sms, h->smem_optin, s));
       else
         PG_CUDA(pg::launch_prune_reverse(pr, false, sms, s));
@@ -1229,7 +1231,7 @@ int pg_autotune(pg_handle h, pg_params* p, const float* d_base, uint32_t d, cons
       rc = try_value(&pg_tuning::hash_factor, f);
       if (rc) return restore(rc);
     }
-    if (tp.screen == PG_SCREEN_BF16) {
+    if (tp.screen != PG_SCREEN_NONE) {
       for (uint32_t c : {50u, 100u, 25u}) {
         rc = try_value(&pg_tuning::screen_carveout, c);
         if (rc) return restore(rc);

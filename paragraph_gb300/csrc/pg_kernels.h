@@ -33,6 +33,7 @@ struct PruneArgs {
   // screened kernel: preferred shared-memory carveout in percent (0 = 76); results do not
   // depend on it
   uint32_t carveout;
+  uint32_t screen_half;  // screened kernel: FP16 operands instead of BF16
 };
 
 struct MergeArgs {

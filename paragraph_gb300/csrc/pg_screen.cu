@@ -1,4 +1,4 @@
-// pg_screen.cu -- screened prune + reverse (K6/K10) with a BF16 tensor-core Gram.
+// pg_screen.cu -- screened prune + reverse (K6/K10) with a BF16 or FP16 tensor-core Gram.
 //
 // Same result as k_prune_reverse (strict rounds), bit for bit.  Per node (one warp, up to 64
 // candidates; up to 96 in the three-slot variant, whose Gram is built in two passes):
@@ -12,13 +12,17 @@
 //   3. the RNG scan of the plain kernel, where each occlusion test dist(p, r) < d_p is decided
 //      from -G[p][r] when it lies farther than the error bound E(p, r) from d_p, and re-scored
 //      with the exact FP32 chain otherwise.
-// Error bound (x, y = FP32 rows, x^ = bf16(x), e_x = x - x^; Cauchy-Schwarz throughout):
+// Error bound (x, y = FP32 rows, x^ = bf16(x) or fp16(x), e_x = x - x^; Cauchy-Schwarz
+// throughout; FP16's 11-bit significand makes |e_x| about 8x smaller than BF16's, so far fewer
+// tests fall inside the margin -- values beyond FP16's range give infinite norms, which send
+// every test of that node to the exact chain):
 //   |sum x^y^ - sum xy| <= |e_x|(|y| + |e_y|) + |x||e_y|
 //   |MMA(x^, y^) - sum x^y^| <= c_acc (|x| + |e_x|)(|y| + |e_y|)   (FP32 accumulation of Dp terms)
 //   |chain(x, y) - sum xy| <= c_seq |x||y|                          (the reference's FP32 chain)
 // with c_acc = (Dp + 32) * 2^-21 and c_seq = (D + 2) * 2^-23 (both several times the textbook
 // gamma_n), plus a 2^-20 relative guard on the comparison itself.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "pg_device.cuh"
 #include "pg_kernels.h"
@@ -27,11 +31,21 @@ namespace pg {
 
 namespace {
 
-__device__ __forceinline__ uint32_t bf16x2_bits(float lo, float hi, float& elo, float& ehi) {
-  const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
-  elo = lo - __low2float(h);
-  ehi = hi - __high2float(h);
-  return *reinterpret_cast<const uint32_t*>(&h);
+// Two floats rounded to the screening type (FP16 when HALF, else BF16), packed; the rounding
+// errors in elo / ehi.
+template <bool HALF>
+__device__ __forceinline__ uint32_t pack2(float lo, float hi, float& elo, float& ehi) {
+  if constexpr (HALF) {
+    const __half2 h = __floats2half2_rn(lo, hi);
+    elo = lo - __low2float(h);
+    ehi = hi - __high2float(h);
+    return *reinterpret_cast<const uint32_t*>(&h);
+  } else {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    elo = lo - __low2float(h);
+    ehi = hi - __high2float(h);
+    return *reinterpret_cast<const uint32_t*>(&h);
+  }
 }
 
 __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
@@ -48,13 +62,22 @@ __device__ __forceinline__ void ldsm_x2(uint32_t (&r)[2], const void* p) {
                : "r"(a));
 }
 
-__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4],
-                                         const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+template <bool HALF>
+__device__ __forceinline__ void mma16(float (&c)[4], const uint32_t (&a)[4],
+                                      const uint32_t (&b)[2]) {
+  if constexpr (HALF) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+  } else {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+  }
 }
 
 __device__ __forceinline__ float key_to_dist(uint64_t key) {
@@ -69,7 +92,7 @@ __host__ __device__ inline uint32_t screen_dp(uint32_t d) { return (d + 15u) / 1
 
 namespace {
 
-constexpr uint32_t kChunkStride = 24;  // BF16 per chunk row: 48 B keeps ldmatrix rows conflict-free
+constexpr uint32_t kChunkStride = 24;  // 16-bit values per chunk row: 48 B keeps ldmatrix rows conflict-free
 
 template <int NS>
 struct ScreenShape {
@@ -79,12 +102,12 @@ struct ScreenShape {
 
 // Per-warp shared memory of the screened kernels.
 struct ScreenSmem {
-  __nv_bfloat16* chunk;  // C x kChunkStride: one K chunk of the BF16 rows
+  uint16_t* chunk;       // C x kChunkStride: one K chunk of the rows in the screening type
   float* G;              // C(C-1)/2: packed strictly-lower Gram
   uint32_t* ids;         // sorted ids
   float* dist;           // sorted exact distances to the node
   float* nrm;            // |x| per original slot
-  float* err;            // |x - bf16(x)| per original slot
+  float* err;            // |x - round(x)| per original slot (BF16 or FP16 rounding)
   uint32_t* orig;        // sorted position -> original slot
   uint32_t* kept_o;      // kept entries: original slot
   uint32_t* kept_i;      // kept entries: id
@@ -94,7 +117,7 @@ template <int NS>
 __device__ __forceinline__ ScreenSmem screen_smem(unsigned char* raw) {
   constexpr uint32_t C = ScreenShape<NS>::kC;
   ScreenSmem m;
-  m.chunk = reinterpret_cast<__nv_bfloat16*>(raw);
+  m.chunk = reinterpret_cast<uint16_t*>(raw);
   m.G = reinterpret_cast<float*>(raw + static_cast<size_t>(C) * kChunkStride * 2);
   m.ids = reinterpret_cast<uint32_t*>(m.G + ScreenShape<NS>::kTri);
   m.dist = reinterpret_cast<float*>(m.ids + C);
@@ -115,7 +138,7 @@ __device__ __forceinline__ uint32_t tri_index(uint32_t r, uint32_t c) {  // r > 
 // 0 .. 2 mt + 1) in registers and storing them packed into sm.G.  The FIRST pass also runs the
 // exact chains dist(b, id[s]) (FLT_MAX where !valid[s]) and the two norms per row.  Lane l owns
 // slots l, 32 + l, ...
-template <int NS, int MT_LO, int MT_HI, bool FIRST>
+template <int NS, int MT_LO, int MT_HI, bool FIRST, bool HALF>
 __device__ __forceinline__ void screen_pass(const float* __restrict__ base, uint32_t d,
                                             const float* __restrict__ brow,
                                             const uint32_t (&id)[NS], const bool (&valid)[NS],
@@ -152,8 +175,8 @@ __device__ __forceinline__ void screen_pass(const float* __restrict__ base, uint
         uint2 packed = make_uint2(0u, 0u);
         if (in) {
           float e0, e1, e2, e3;
-          packed.x = bf16x2_bits(v.x, v.y, e0, e1);
-          packed.y = bf16x2_bits(v.z, v.w, e2, e3);
+          packed.x = pack2<HALF>(v.x, v.y, e0, e1);
+          packed.y = pack2<HALF>(v.z, v.w, e2, e3);
           if (FIRST) {
             acc[s] = fmaf(u.x, v.x, acc[s]);
             acc[s] = fmaf(u.y, v.y, acc[s]);
@@ -177,7 +200,7 @@ __device__ __forceinline__ void screen_pass(const float* __restrict__ base, uint
       for (int nt = 0; nt <= 2 * mt + 1; nt++) {
         uint32_t bf[2];
         ldsm_x2(bf, sm.chunk + (8 * nt + (lane & 7u)) * kChunkStride + ((lane >> 3) & 1u) * 8);
-        mma_bf16(gm[mt * (mt + 1) - MT_LO * (MT_LO + 1) + nt], af, bf);
+        mma16<HALF>(gm[mt * (mt + 1) - MT_LO * (MT_LO + 1) + nt], af, bf);
       }
     }
     __syncwarp();
@@ -206,17 +229,17 @@ __device__ __forceinline__ void screen_pass(const float* __restrict__ base, uint
 
 // Steps 1 and 2: exact chains, norms and the whole lower-triangle Gram of the 32 NS slots (two
 // register passes for 96 candidates: row blocks 0-3, then 4-5).
-template <int NS>
+template <int NS, bool HALF>
 __device__ __forceinline__ void screen_rows_and_gram(const float* __restrict__ base, uint32_t d,
                                                      const float* __restrict__ brow,
                                                      const uint32_t (&id)[NS],
                                                      const bool (&valid)[NS],
                                                      const ScreenSmem& sm, float (&dist)[NS]) {
   if constexpr (NS == 2) {
-    screen_pass<2, 0, 4, true>(base, d, brow, id, valid, sm, dist);
+    screen_pass<2, 0, 4, true, HALF>(base, d, brow, id, valid, sm, dist);
   } else {
-    screen_pass<3, 0, 4, true>(base, d, brow, id, valid, sm, dist);
-    screen_pass<3, 4, 6, false>(base, d, brow, id, valid, sm, dist);
+    screen_pass<3, 0, 4, true, HALF>(base, d, brow, id, valid, sm, dist);
+    screen_pass<3, 4, 6, false, HALF>(base, d, brow, id, valid, sm, dist);
   }
 }
 
@@ -300,7 +323,7 @@ __device__ __forceinline__ bool screen_occluded(const float* __restrict__ base, 
 template <int NS>
 size_t screen_smem_ns() {
   constexpr size_t C = ScreenShape<NS>::kC;
-  return C * kChunkStride * 2                          // one K chunk of the BF16 rows
+  return C * kChunkStride * 2                          // one K chunk of the 16-bit rows
          + static_cast<size_t>(ScreenShape<NS>::kTri) * 4  // G, strictly lower triangle
          + C * 4 * 7;                                  // ids, dist, |x|, |e|, slot, kept x2
 }
@@ -311,7 +334,7 @@ bool screen_supported(uint32_t c, uint32_t d, int strict) {
   return strict && c <= ScreenShape<3>::kC && d >= 4 && d <= 1024 && (d % 4) == 0;
 }
 
-template <int NS>
+template <int NS, bool HALF>
 __global__ void __launch_bounds__(32, NS == 2 ? 16 : 8) k_prune_screen(PruneArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const ScreenSmem sm = screen_smem<NS>(smem_raw);
@@ -335,7 +358,7 @@ __global__ void __launch_bounds__(32, NS == 2 ? 16 : 8) k_prune_screen(PruneArgs
       valid[s] = (x != kTomb && x != static_cast<uint32_t>(b) && x != kMaskedTomb);
     }
     float dist[NS];
-    screen_rows_and_gram<NS>(a.base, d, a.base + b * d, id, valid, sm, dist);
+    screen_rows_and_gram<NS, HALF>(a.base, d, a.base + b * d, id, valid, sm, dist);
     uint32_t nv = 0;
 #pragma unroll
     for (int s = 0; s < NS; s++) nv += __popc(__ballot_sync(kFull, valid[s]));  // all lanes
@@ -415,11 +438,16 @@ cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_opt
                                 cudaStream_t st) {
   if (!screen_supported(a.c, a.d, a.strict)) return cudaErrorInvalidValue;
   if (a.carveout > 100) return cudaErrorInvalidValue;
+  const bool half = a.screen_half != 0;
   if (a.c <= ScreenShape<2>::kC)
-    return launch_screen_kernel(k_prune_screen<2>, a, a.n, screen_smem_ns<2>(), a.carveout,
-                                num_sms, smem_optin, st);
-  return launch_screen_kernel(k_prune_screen<3>, a, a.n, screen_smem_ns<3>(), a.carveout,
-                              num_sms, smem_optin, st);
+    return half ? launch_screen_kernel(k_prune_screen<2, true>, a, a.n, screen_smem_ns<2>(),
+                                       a.carveout, num_sms, smem_optin, st)
+                : launch_screen_kernel(k_prune_screen<2, false>, a, a.n, screen_smem_ns<2>(),
+                                       a.carveout, num_sms, smem_optin, st);
+  return half ? launch_screen_kernel(k_prune_screen<3, true>, a, a.n, screen_smem_ns<3>(),
+                                     a.carveout, num_sms, smem_optin, st)
+              : launch_screen_kernel(k_prune_screen<3, false>, a, a.n, screen_smem_ns<3>(),
+                                     a.carveout, num_sms, smem_optin, st);
 }
 
 }  // namespace pg

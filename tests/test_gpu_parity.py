@@ -236,11 +236,12 @@ def test_screened_build_matches_plain_and_oracle_fixture(pg, handle, golden_dir,
     assert st.evals_total == ref["stats"]["evals_total"]
 
 
+@pytest.mark.parametrize("screen", [1, 3])  # BF16, FP16
 @pytest.mark.parametrize("n,d,seed", [(20000, 200, 1), (6000, 64, 7), (3000, 8, 8)])
-def test_screened_build_matches_oracle(pg, handle, n, d, seed):
+def test_screened_build_matches_oracle(pg, handle, n, d, seed, screen):
     from paragraph_gb300 import datagen
     base, gt = datagen.make_dataset(n, d, seed=seed)
-    g, p, st, ref = _build_both(pg, handle, base, gt, screen=pg.SCREEN_BF16)
+    g, p, st, ref = _build_both(pg, handle, base, gt, screen=screen)
     assert np.array_equal(p, ref["proj"])
     bad = (g != ref["graph"]).any(axis=1)
     assert not bad.any(), f"{bad.sum()} rows differ"
@@ -249,23 +250,24 @@ def test_screened_build_matches_oracle(pg, handle, n, d, seed):
     assert sum(st.rescored) < 0.5 * sum(st.evals_prune)
 
 
-def test_screened_build_with_hubs_and_duplicates(pg, handle, golden_dir):
+@pytest.mark.parametrize("screen", [1, 3])
+def test_screened_build_with_hubs_and_duplicates(pg, handle, golden_dir, screen):
     """Exact duplicate vectors give exact ties and zero-width gaps: the screen must defer every
     such decision to the exact chain."""
     f = load(golden_dir, "edge")
-    g, p, st, ref = _build_both(pg, handle, f["base"], f["gt"], screen=pg.SCREEN_BF16)
+    g, p, st, ref = _build_both(pg, handle, f["base"], f["gt"], screen=screen)
     assert np.array_equal(g, ref["graph"])
 
 
+@pytest.mark.parametrize("screen", [1, 3])  # BF16, FP16
 @pytest.mark.parametrize("n,d,degree,seed,cosine", [(8000, 512, 48, 5, True),
                                                     (6000, 200, 32, 6, False)])
-def test_screened_build_96_candidates(pg, handle, n, d, degree, seed, cosine):
+def test_screened_build_96_candidates(pg, handle, n, d, degree, seed, cosine, screen):
     """L = 96: the screened prune's three-slot variant (96 candidates, Gram in two passes)."""
     from paragraph_gb300 import datagen
     base, q = datagen.make_base_queries(n, d, seed=seed, cosine=cosine)
     gt = datagen.ground_truth(base, q, 128)
-    g, p, st, ref = _build_both(pg, handle, base, gt, degree=degree, beam=96,
-                                screen=pg.SCREEN_BF16)
+    g, p, st, ref = _build_both(pg, handle, base, gt, degree=degree, beam=96, screen=screen)
     assert np.array_equal(p, ref["proj"])
     bad = (g != ref["graph"]).any(axis=1)
     assert not bad.any(), f"{bad.sum()} rows differ"
@@ -273,9 +275,10 @@ def test_screened_build_96_candidates(pg, handle, n, d, degree, seed, cosine):
     assert sum(st.rescored) < 0.5 * sum(st.evals_prune)
 
 
-def test_screened_96_with_hubs_and_duplicates(pg, handle, golden_dir):
+@pytest.mark.parametrize("screen", [1, 3])
+def test_screened_96_with_hubs_and_duplicates(pg, handle, golden_dir, screen):
     f = load(golden_dir, "edge")
     g, p, st, ref = _build_both(pg, handle, f["base"], f["gt"], degree=32, beam=96,
-                                screen=pg.SCREEN_BF16)
+                                screen=screen)
     assert np.array_equal(g, ref["graph"])
     assert st.evals_total == ref["stats"]["evals_total"]

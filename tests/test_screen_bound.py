@@ -35,6 +35,38 @@ def e4m3(x: np.ndarray) -> np.ndarray:
     return (np.clip(q, -448, 448) * scale).astype(np.float64)
 
 
+def fp16(x: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(x, dtype=np.float32).astype(np.float16).astype(np.float32)
+
+
+def test_fp16_screen_bound_holds(golden_dir):
+    """The same bound with FP16 rounding (the PG_SCREEN_FP16 path): e = x - fp16(x)."""
+    f = np.load(os.path.join(golden_dir, "ref_edge_1000x200.npz"))
+    x = f["base"].astype(np.float32)
+    n, d = x.shape
+    rng = np.random.default_rng(1)
+    pairs = rng.integers(0, n, (6000, 2))
+    xh = fp16(x).astype(np.float64)
+    x64 = x.astype(np.float64)
+    err = x64 - xh
+    nrm = np.sqrt((x64 ** 2).sum(1)) * 1.0001
+    enrm = np.sqrt((err ** 2).sum(1)) * 1.0001
+    dp = (d + 15) // 16 * 16
+    c_acc = (dp + 32) * 2.0 ** -21
+    c_seq = (d + 2) * 2.0 ** -23
+    i, j = pairs[:, 0], pairs[:, 1]
+    s64 = (x64[i] * x64[j]).sum(1)
+    shat = (xh[i] * xh[j]).sum(1)
+    chain = np.array([-float(oracle.dist_seq(x, int(a), int(b))) for a, b in pairs])
+    bound = (enrm[i] * (nrm[j] + enrm[j]) + nrm[i] * enrm[j]
+             + c_acc * (nrm[i] + enrm[i]) * (nrm[j] + enrm[j]) + c_seq * nrm[i] * nrm[j])
+    assert (np.abs(shat - chain) <= bound).all()
+    nz = (nrm[i] > 0) & (nrm[j] > 0)
+    rel = np.abs(shat - s64)[nz] / (nrm[i] * nrm[j])[nz]
+    print(f"max |s-s64|/(|x||y|): fp16 {rel.max():.3e}")
+    assert rel.max() < 2.0 ** -10
+
+
 def test_bf16_screen_bound_holds_and_error_is_stated(golden_dir):
     f = np.load(os.path.join(golden_dir, "ref_edge_1000x200.npz"))  # includes hubs, duplicates
     x = f["base"].astype(np.float32)
