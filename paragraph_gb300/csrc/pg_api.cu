@@ -71,7 +71,7 @@ size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
 struct Layout {
   size_t winner, pruned, pruned_num, indeg, offs, tile_sums, cursor, edges, rev, rev_num, sres,
-      proj, graph, segs, total;
+      proj, graph, segs, norms, total;
 };
 
 Layout make_layout(uint64_t n, uint32_t pmax, uint32_t rmax, uint32_t L, uint32_t proj_deg,
@@ -97,6 +97,7 @@ Layout make_layout(uint64_t n, uint32_t pmax, uint32_t rmax, uint32_t L, uint32_
   l.proj = take(n * proj_deg * 4);
   l.graph = take(n * degree * 4);
   l.segs = take(2 * (static_cast<size_t>(seg_count) + 1) * 8);
+  l.norms = take(n * 8);  // screened prune: per-point norm bounds
   l.total = o;
   return l;
 }
@@ -275,6 +276,8 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
   uint32_t* rnum = reinterpret_cast<uint32_t*>(w + lay.rev_num);
   uint32_t* sres = reinterpret_cast<uint32_t*>(w + lay.sres);
   uint32_t* proj = proj_out ? proj_out : reinterpret_cast<uint32_t*>(w + lay.proj);
+  float2* norms = reinterpret_cast<float2*>(w + lay.norms);
+  const bool screened = p->screen != PG_SCREEN_NONE && pg::screen_supported(L, d, 1);
   unsigned long long* cnt = h->d_counters;
   const int sms = h->num_sms;
   uint64_t* d_seg = nullptr;
@@ -400,9 +403,12 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
       pr.rescored = cnt + C_RESCORED + r;
       pr.carveout = h->tune.screen_carveout;
       pr.screen_half = p->screen == PG_SCREEN_FP16;
-      if (p->screen != PG_SCREEN_NONE && pg::screen_supported(pr.c, d, pr.strict))
+      pr.norms = norms;
+      if (screened) {
+        if (r == 0)
+          PG_CUDA(pg::launch_screen_norms(base, n, d, pr.screen_half, norms, sms, s));
         PG_CUDA(pg::launch_prune_screen(pr, sms, h->smem_optin, s));
-      else
+      } else
         PG_CUDA(pg::launch_prune_reverse(pr, false, sms, s));
       PG_CUDA(pg::launch_reverse_csr(pruned, pnum, p->degree, n, indeg, offs, tsum, cursor, edges,
                                      sms, s));

@@ -20,6 +20,15 @@ enum : uint32_t {
   kErrCapacity = 1u << 3,  // a list exceeded the capacity a kernel was built for
 };
 
+// 32 bytes of read-only global memory in one 256-bit load (p 32-byte aligned): one L1 wavefront
+// per sector where two 16-byte loads take two.
+__device__ __forceinline__ void ld8(const float* p, float (&v)[8]) {
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]),
+        "=f"(v[7])
+      : "l"(p));
+}
+
 // One FMA chain over d = 0..D-1: distance_between (Gbuilder.cuh:785-797), -(sum x[d]*y[d]).
 // Rows are 16-byte aligned when D % 4 == 0 (the library checks), so float4 loads keep the order.
 __device__ __forceinline__ float dist_seq(const float* __restrict__ x, const float* __restrict__ y,

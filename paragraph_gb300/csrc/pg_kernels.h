@@ -34,6 +34,9 @@ struct PruneArgs {
   // depend on it
   uint32_t carveout;
   uint32_t screen_half;  // screened kernel: FP16 operands instead of BF16
+  // screened kernel: per point (|x|, |x - x^| + |x^_sub|) upper bounds from launch_screen_norms
+  // with the same screen_half
+  const float2* norms;
 };
 
 struct MergeArgs {
@@ -171,6 +174,9 @@ cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, c
 bool search_supported(uint32_t d, uint32_t km, uint32_t kp, uint32_t kd);
 // Screened (BF16 tensor-core Gram + exact re-scoring) prune for strict rounds, c <= 64, d <= 256.
 bool screen_supported(uint32_t c, uint32_t d, int strict);
+// Per-point norm bounds for the screened prune (FP16 rounding when half, else BF16): n float2.
+cudaError_t launch_screen_norms(const float* base, uint64_t n, uint32_t d, uint32_t half,
+                                float2* out, int num_sms, cudaStream_t st);
 size_t screen_smem_per_warp(uint32_t d);
 cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_optin,
                                 cudaStream_t st);

@@ -250,6 +250,24 @@ def test_screened_build_matches_oracle(pg, handle, n, d, seed, screen):
     assert sum(st.rescored) < 0.5 * sum(st.evals_prune)
 
 
+@pytest.mark.parametrize("screen", [1, 3])  # BF16, FP16
+def test_screened_build_extreme_scales(pg, handle, screen):
+    """Points scaled by 1e-6 .. 1e5: FP16 copies with subnormal coordinates (the norm bounds carry
+    their norm, in case the tensor core flushes them) and coordinates beyond FP16's range (infinite
+    norm bounds: every test of such a point goes to the exact chain).  Edges still equal the
+    oracle's."""
+    from paragraph_gb300 import datagen
+    base, gt = datagen.make_dataset(3000, 64, seed=9)
+    f = 10.0 ** np.random.default_rng(9).uniform(-6, 5, base.shape[0])
+    base = np.ascontiguousarray(base * f[:, None].astype(np.float32), dtype=np.float32)
+    assert np.isfinite(base).all() and (np.abs(base) > 65504).any()
+    g, p, st, ref = _build_both(pg, handle, base, gt, screen=screen)
+    assert np.array_equal(p, ref["proj"])
+    bad = (g != ref["graph"]).any(axis=1)
+    assert not bad.any(), f"{bad.sum()} rows differ"
+    assert st.evals_total == ref["stats"]["evals_total"]
+
+
 @pytest.mark.parametrize("screen", [1, 3])
 def test_screened_build_with_hubs_and_duplicates(pg, handle, golden_dir, screen):
     """Exact duplicate vectors give exact ties and zero-width gaps: the screen must defer every
