@@ -533,6 +533,48 @@ __global__ void __launch_bounds__(256) k_reverse_lists(const uint32_t* __restric
   }
 }
 
+// One node's merged list (reverse entries, then pruned entries) with exact distances to the node,
+// sorted by (distance, position) into ids_s / dist_s[0 .. nn); E = slots per lane (nn <= 32 E).
+template <int E>
+__device__ __forceinline__ void merge_gather_sort(const MergeArgs& a, uint64_t b, uint32_t rn,
+                                                  uint32_t nn, uint32_t* ids_s, float* dist_s) {
+  const uint32_t lane = lane_id();
+  uint32_t id[E];
+  bool valid[E];
+#pragma unroll
+  for (int s = 0; s < E; s++) {
+    const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+    uint32_t x = kTomb;
+    if (j < rn)
+      x = a.reverse[b * a.r + j];
+    else if (j < nn)
+      x = a.pruned[b * a.p + (j - rn)];
+    if (j < nn && x >= a.n) {  // out-of-range input id
+      raise_error(a.status, kErrBadId);
+      x = kTomb;
+    }
+    id[s] = x;
+    valid[s] = j < nn && x != kTomb;
+  }
+  float dist[E];
+  dist_seq_multi<E>(a.base + b * a.d, a.base, a.d, id, valid, dist);
+  uint64_t key[E];
+#pragma unroll
+  for (int s = 0; s < E; s++) {
+    const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
+    key[s] = (j < nn) ? pack_key(dist[s], j) : ~0ull;
+  }
+  warp_sort_kv<E>(key, id);
+#pragma unroll
+  for (int s = 0; s < E; s++) {
+    const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
+    if (i < nn) {
+      ids_s[i] = id[s];
+      dist_s[i] = key_dist(key[s]);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ K3: merge + prune
 // fusion_merge_sort_prune_kernel (Gbuilder.cuh:1467-1601): merged list = reverse entries then
 // pruned entries (pr_sort_list view); sort by distance keeping that order on ties; RNG prune
@@ -560,41 +602,14 @@ __global__ void __launch_bounds__(256) k_merge_prune(MergeArgs a) {
       for (uint32_t t = lane; t < a.degree; t += 32) orow[t] = kTomb;
       continue;
     }
-    uint32_t id[E];
-    bool valid[E];
-#pragma unroll
-    for (int s = 0; s < E; s++) {
-      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
-      uint32_t x = kTomb;
-      if (j < rn)
-        x = a.reverse[b * a.r + j];
-      else if (j < nn)
-        x = a.pruned[b * a.p + (j - rn)];
-      if (j < nn && x >= a.n) {  // out-of-range input id
-        raise_error(a.status, kErrBadId);
-        x = kTomb;
-      }
-      id[s] = x;
-      valid[s] = j < nn && x != kTomb;
-    }
-    float dist[E];
-    dist_seq_multi<E>(a.base + b * a.d, a.base, a.d, id, valid, dist);
-    uint64_t key[E];
-#pragma unroll
-    for (int s = 0; s < E; s++) {
-      const uint32_t j = static_cast<uint32_t>(s) * 32u + lane;
-      key[s] = (j < nn) ? pack_key(dist[s], j) : ~0ull;
-    }
     if (lane == 0) ev += nn;
-    warp_sort_kv<E>(key, id);
-#pragma unroll
-    for (int s = 0; s < E; s++) {
-      const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
-      if (i < nn) {
-        ids_s[i] = id[s];
-        dist_s[i] = key_dist(key[s]);
-      }
-    }
+    // the merged lists are mostly short: size the distance slots and the sort to this one
+    if (nn <= 32)
+      merge_gather_sort<1>(a, b, rn, nn, ids_s, dist_s);
+    else if (E >= 2 && nn <= 64)
+      merge_gather_sort<(E >= 2 ? 2 : 1)>(a, b, rn, nn, ids_s, dist_s);
+    else
+      merge_gather_sort<E>(a, b, rn, nn, ids_s, dist_s);
     __syncwarp();
     if (lane == 0) out_s[0] = ids_s[0];
     __syncwarp();
