@@ -34,12 +34,17 @@ sys.path.insert(0, ROOT)
 UNIT = "evals/s"
 
 
-def metric_name(args) -> str:
+def metric_name(args, total: int | None = None) -> str:
     """The metric string of the workload the arguments describe (the 1M x 200 inner-product,
-    M = 32, L = 64 build by default)."""
-    n = "1M" if args.n == 1_000_000 else str(args.n)
+    M = 32, L = 64 build by default; `total` points over args.batched sub-indexes for the batched
+    form)."""
     kind = "cosine" if args.cosine else "IP"
-    return (f"distance_evals_per_s (build, {n}x{args.d} {kind}, M={args.degree}, L={args.beam}, "
+    if args.batched:
+        what = f"batched build, {args.batched} sub-indexes, {total}x{args.d} {kind}"
+    else:
+        n = "1M" if args.n == 1_000_000 else str(args.n)
+        what = f"build, {n}x{args.d} {kind}"
+    return (f"distance_evals_per_s ({what}, M={args.degree}, L={args.beam}, "
             "screened vs FP32, identical edges)")
 
 
@@ -207,7 +212,7 @@ def cpu_baseline_sample(args, base_np, gt_np, seconds):
     """The oracle (CPU restatement of K0..K11, all host threads) on the workload.  When the whole
     build fits the time budget (judged from a 1% pilot of the search) it runs the complete build;
     otherwise phase 1 plus the round-1 search over as many queries as fit.  Returns
-    (evals/s, description, threads)."""
+    (evals/s, description, threads, the full build's oracle result or None)."""
     import oracle
     t0 = time.perf_counter()
     p1 = oracle.build_graph(base_np, gt_np, degree=args.degree, beam=args.beam, link_rounds=0)
@@ -257,15 +262,20 @@ def run_reference(args):
     vals = []
     desc = ""
     threads = 1
+    full_evals = None
     steps = max(args.steps, 1)
     per_step = max(min(args.cpu_seconds, 120.0 / (steps + args.warmup)), 3.0)
     for i in range(args.warmup + steps):
-        v, desc, threads, _ = cpu_baseline_sample(args, base_np, gt_np, per_step)
+        v, desc, threads, full = cpu_baseline_sample(args, base_np, gt_np, per_step)
+        if full is not None:
+            full_evals = full["stats"]["evals_total"]
         if i >= args.warmup:
             vals.append(v)
     value = statistics.mean(vals)
+    # one full build at the measured rate (the sample is the whole build when it fits the budget)
+    ms_step = round(full_evals / value * 1e3, 1) if full_evals else None
     line = {"metric": metric_name(args), "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": None,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded mixture-of-Gaussians stand-in for T2I-style data)",
             "config": {"workload": f"ParaGraph build {args.n}x{args.d} IP, gt top-128, "
@@ -545,7 +555,7 @@ def run_batched(args):
     torch.cuda.synchronize()
     ms_alone = a.elapsed_time(b_)
     identical = bool(torch.equal(graph, alone))
-    line = {"metric": metric_name(args) + " -- batched form", "value": st.evals_total / (ms / 1e3),
+    line = {"metric": metric_name(args, total), "value": st.evals_total / (ms / 1e3),
             "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if args.screen == "none" else "f32+" + args.screen,
