@@ -72,13 +72,6 @@ __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
                : "r"(a));
 }
 
-__device__ __forceinline__ void ldsm_x2(uint32_t (&r)[2], const void* p) {
-  const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
-  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];"
-               : "=r"(r[0]), "=r"(r[1])
-               : "r"(a));
-}
-
 template <bool HALF>
 __device__ __forceinline__ void mma16(float (&c)[4], const uint32_t (&a)[4],
                                       const uint32_t (&b)[2]) {
@@ -236,15 +229,19 @@ __device__ __forceinline__ void screen_pass(const float* __restrict__ base, uint
     }
     }
     __syncwarp();
+    // A fragments of row blocks 0 .. MT_HI-1.  G = A A^T, so the B fragment of column tile nt
+    // (rows 8 nt .. 8 nt + 7 as the n index) is half of an A fragment already held: (a0, a2) of
+    // block nt / 2 for even nt, (a1, a3) for odd nt -- one ldmatrix.x4 per row block and chunk.
+    uint32_t af[MT_HI][4];
+#pragma unroll
+    for (int mt = 0; mt < MT_HI; mt++)
+      ldsm_x4(af[mt], sm.chunk + (16 * mt + (lane & 15u)) * kChunkStride + (lane >> 4) * 8);
 #pragma unroll
     for (int mt = MT_LO; mt < MT_HI; mt++) {
-      uint32_t af[4];
-      ldsm_x4(af, sm.chunk + (16 * mt + (lane & 15u)) * kChunkStride + (lane >> 4) * 8);
 #pragma unroll
       for (int nt = 0; nt <= 2 * mt + 1; nt++) {
-        uint32_t bf[2];
-        ldsm_x2(bf, sm.chunk + (8 * nt + (lane & 7u)) * kChunkStride + ((lane >> 3) & 1u) * 8);
-        mma16<HALF>(gm[mt * (mt + 1) - MT_LO * (MT_LO + 1) + nt], af, bf);
+        const uint32_t bf[2] = {af[nt >> 1][nt & 1], af[nt >> 1][(nt & 1) + 2]};
+        mma16<HALF>(gm[mt * (mt + 1) - MT_LO * (MT_LO + 1) + nt], af[mt], bf);
       }
     }
     __syncwarp();
