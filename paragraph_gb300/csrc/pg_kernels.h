@@ -172,12 +172,12 @@ cudaError_t launch_merge_prune(const MergeArgs& a, int num_sms, cudaStream_t st)
 // (see search_supported).
 cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, cudaStream_t st);
 bool search_supported(uint32_t d, uint32_t km, uint32_t kp, uint32_t kd);
-// Screened (BF16 tensor-core Gram + exact re-scoring) prune for strict rounds, c <= 64, d <= 256.
+// Screened (FP16 or BF16 tensor-core Gram + exact re-scoring) prune for strict rounds,
+// c <= 96, 4 <= d <= 1024, d % 4 == 0.
 bool screen_supported(uint32_t c, uint32_t d, int strict);
 // Per-point norm bounds for the screened prune (FP16 rounding when half, else BF16): n float2.
 cudaError_t launch_screen_norms(const float* base, uint64_t n, uint32_t d, uint32_t half,
                                 float2* out, int num_sms, cudaStream_t st);
-size_t screen_smem_per_warp(uint32_t d);
 cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_optin,
                                 cudaStream_t st);
 

@@ -416,8 +416,6 @@ size_t screen_smem_ns() {
          + C * 4 * 7;                                  // ids, dist, |x|, |e|, slot, kept x2
 }
 
-size_t screen_smem_per_warp(uint32_t /*d*/) { return screen_smem_ns<2>(); }
-
 bool screen_supported(uint32_t c, uint32_t d, int strict) {
   return strict && c <= ScreenShape<3>::kC && d >= 4 && d <= 1024 && (d % 4) == 0;
 }
