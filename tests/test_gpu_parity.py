@@ -183,6 +183,20 @@ def test_build_host_equals_build_device(pg, handle, golden_dir):
     assert st.evals_total == st2.evals_total
 
 
+@pytest.mark.parametrize("n,d,seed", [(3001, 8, 21), (2999, 200, 22)])
+def test_build_host_copy_split(pg, handle, n, d, seed):
+    """pg_build_host splits the input bytes over two copy streams: D=8 puts all of base on the
+    first and gt on the second (gt is the larger), D=200 splits base itself; odd n makes the
+    split point fall inside a row.  Both equal the device-resident build and the oracle."""
+    from paragraph_gb300 import datagen
+    base, gt = datagen.make_dataset(n, d, seed=seed)
+    g_host, p_host, st = handle.build_host(base, gt, pg.default_params(32, 64))
+    g_dev, p_dev, _, ref = _build_both(pg, handle, base, gt)
+    assert np.array_equal(g_host, g_dev) and np.array_equal(p_host, p_dev)
+    assert np.array_equal(g_host, ref["graph"])
+    assert st.h2d_bytes == base.nbytes + gt.nbytes
+
+
 def test_builder_facade_and_savegraph(pg, golden_dir, tmp_path):
     f = load(golden_dir, "mix")
     b = pg.Builder(f["base"], f["gt"])
