@@ -528,7 +528,9 @@ int blocks_for(uint64_t warps, int per_block, int num_sms, int per_sm) {
 uint32_t gt_max_k() { return 256; }
 
 size_t gt_chunk_rows(uint64_t n, uint64_t nq) {
-  uint64_t cq = (2ull << 30) / (4 * n);  // a 2 GB score block
+  // an 8 GB score block: 2048 query rows per chunk at n = 1M (each chunk's GEMM re-reads the
+  // FP16 base, so larger chunks read it fewer times and give the GEMM a wider N)
+  uint64_t cq = (8ull << 30) / (4 * n);
   if (cq < 1) cq = 1;
   if (cq > 4096) cq = 4096;
   if (cq > nq) cq = nq;
