@@ -210,7 +210,7 @@ def search_roofline(st, args, peak_gbs, peak_kind, rounds):
 
 def cpu_baseline_sample(args, base_np, gt_np, seconds):
     """The oracle (CPU restatement of K0..K11, all host threads) on the workload.  When the whole
-    build fits the time budget (judged from a 1% pilot of the search) it runs the complete build;
+    build fits the time budget (estimated from a 1% pilot of the search) it runs the complete build;
     otherwise phase 1 plus the round-1 search over as many queries as fit.  Returns
     (evals/s, description, threads, the full build's oracle result or None)."""
     import oracle
@@ -361,8 +361,9 @@ def run_ours(args):
                       "identical_edges": bool(torch.equal(graph, graph2) and torch.equal(proj, proj2)),
                       "speedup_of_timed_path": round(oms / (ms_total / args.steps), 3)}
         del graph2, proj2
-    # the driver's whole index: this build plus the CPU RoarGraph path (six MatchSup rounds,
-    # FusionNN) and FusionFinal, all on the GPU (pg_build_index)
+    # the reference driver's whole index (tests/test_t2iend.cu): the GPU build plus the CPU
+    # RoarGraph path (six MatchSup rounds, FusionNN) and FusionFinal, all on the GPU
+    # (pg_build_index)
     index_line = None
     if not args.no_index:
         iout = torch.empty((n, 2 * 40 + 70), dtype=torch.int32, device=dev)

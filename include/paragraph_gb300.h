@@ -161,8 +161,9 @@ int pg_build_batched_device(pg_handle h, const pg_params* p, const float* d_base
  * pg_match_sup: MatchSup (:365-488) round `topn` (1-based rank of the matched ground-truth id):
  *   out n x m_nn, cnt n.  gt: q x gt_k, ids >= n end a row (the reference's padding).
  * pg_fusion_nn: FusionNN (:490-537) over `rounds` MatchSup outputs (rounds x n x m_nn ids and
- *   rounds x n counts, round order as the driver's :912-921); MatchNN's own graph is empty in the
- *   reference (its graph-building loop is commented out, :234-306).  out n x 2*m_nn.
+ *   rounds x n counts, round order as the reference driver's :912-921); MatchNN's own graph is
+ *   empty in the reference (its graph-building loop is commented out, :234-306).  out
+ *   n x 2*m_nn.
  * pg_fusion_final: FusionFinal (:539-613).  Bipartite lists (the FusionNN graph) as CSR
  *   (d_bip_off, n + 1 offsets) or as rows of bip_stride with counts (d_bip_off NULL); supply =
  *   the projection (n x m_supply), link = the link graph (n x m_link).  Row i of out (stride
@@ -170,8 +171,8 @@ int pg_build_batched_device(pg_handle h, const pg_params* p, const float* d_base
  *   the call return PG_EUNSUPPORTED.
  * pg_build_index: the reference driver's whole index (test_t2iend.cu:974-1229): the GPU build
  *   (K0..K11), `match_rounds` MatchSup rounds (topn 1..match_rounds), FusionNN(m_nn) and
- *   FusionFinal(m_supply = proj_degree, m_link = degree, m_final).  The driver's values are
- *   match_rounds 6, m_nn 40, m_final 70; out_stride >= 2*m_nn + m_final.  The entry point is
+ *   FusionFinal(m_supply = proj_degree, m_link = degree, m_final).  The reference driver's
+ *   values are match_rounds 6, m_nn 40, m_final 70; out_stride >= 2*m_nn + m_final.  The entry point is
  *   pg_entry_point of the host ground truth. */
 int pg_match_sup(pg_handle h, const float* d_base, uint64_t n, uint32_t d, const uint32_t* d_gt,
                  uint64_t q, uint32_t gt_k, uint32_t topn, uint32_t m_nn, uint32_t* d_out,

@@ -328,8 +328,8 @@ class Handle:
 
     def build_index(self, base, gt, out, cnt, params: Params | None = None,
                     match_rounds: int = 6, m_nn: int = 40, m_final: int = 70) -> Stats:
-        """pg_build_index: the driver's whole index (GPU build + MatchSup rounds + FusionNN +
-        FusionFinal); out n x stride (>= 2*m_nn + m_final), cnt n."""
+        """pg_build_index: the reference driver's whole index (GPU build + MatchSup rounds +
+        FusionNN + FusionFinal); out n x stride (>= 2*m_nn + m_final), cnt n."""
         params = params or default_params()
         n, d = base.shape
         st = Stats()

@@ -10,7 +10,7 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
-    config.addinivalue_line("markers", "slow: large GPU case (full BASELINE-size workload)")
+    config.addinivalue_line("markers", "slow: large GPU case (the full 1M-point workload)")
 
 
 @pytest.fixture(scope="session")

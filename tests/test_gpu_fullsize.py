@@ -74,8 +74,8 @@ def test_full_size_screened_build_is_identical(workload):
 
 
 def test_full_size_index_matches_oracle(workload):
-    """pg_build_index at 1M x 200 (the driver's whole index: GPU build, six MatchSup rounds,
-    FusionNN, FusionFinal) against the oracle's pipeline, list for list."""
+    """pg_build_index at 1M x 200 (the reference driver's whole index: GPU build, six MatchSup
+    rounds, FusionNN, FusionFinal) against the oracle's pipeline, list for list."""
     import paragraph_gb300 as pg
     base, gt = workload
     params = pg.default_params(32, 64, screen=pg.SCREEN_BF16)

@@ -1,5 +1,5 @@
 """The N > 1 path of bench.py on CPU: two ranks over gloo (127.0.0.1).  The build does not shard
-(one index per GPU; the benchmark spec fixes a single GPU), so N ranks run independent replicas and the
+(one index is built on one GPU), so N ranks run independent replicas and the
 only cross-rank operations are the barrier and the max of the per-rank times."""
 import json
 import os
