@@ -311,10 +311,11 @@ def run_ours(args):
     proj = torch.empty((n, 16), dtype=torch.int32, device=dev)
     stream = torch.cuda.Stream(dev)
     h = pg.Handle(local, stream=stream)
-    # K0, K2 + CSR (5), K3 = 8; per link round search, prune + CSR (5), merge = 8; a screened build
-    # adds the norm pre-pass once
-    screened_launch = 1 if (screen and params.link_rounds > 0 and args.beam <= 96) else 0
-    launches_per_build = 8 + 8 * params.link_rounds + screened_launch
+    # K0, K2 + CSR (5), K3 = 8; per link round search, prune + CSR (5), merge = 8; once per build
+    # the seed-distance pass and, when screened, the norm pre-pass
+    once = (1 if params.link_rounds > 0 else 0) + (
+        1 if (screen and params.link_rounds > 0 and args.beam <= 96) else 0)
+    launches_per_build = 8 + 8 * params.link_rounds + once
     tuning = None
     if args.autotune:
         t0 = time.perf_counter()
@@ -577,6 +578,7 @@ def run_batched(args):
                              "definition": "exact FP64 inner products (pg_ground_truth)"},
             "data_generation_s": round(gen_s, 1), "tuning": tuning,
             "gpu_launches": (10 + 8 * params.link_rounds
+                             + (1 if params.link_rounds > 0 else 0)
                              + (1 if screen and params.link_rounds > 0 and args.beam <= 96 else 0))
                             * args.steps, "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)

@@ -71,7 +71,7 @@ size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
 struct Layout {
   size_t winner, pruned, pruned_num, indeg, offs, tile_sums, cursor, edges, rev, rev_num, sres,
-      proj, graph, segs, norms, total;
+      proj, graph, segs, norms, seeds, total;
 };
 
 Layout make_layout(uint64_t n, uint32_t pmax, uint32_t rmax, uint32_t L, uint32_t proj_deg,
@@ -98,6 +98,7 @@ Layout make_layout(uint64_t n, uint32_t pmax, uint32_t rmax, uint32_t L, uint32_
   l.graph = take(n * degree * 4);
   l.segs = take(2 * (static_cast<size_t>(seg_count) + 1) * 8);
   l.norms = take(n * 8);  // screened prune: per-point norm bounds
+  l.seeds = take(n * 32 * 4);  // link-round searches: every query's 32 seed distances
   l.total = o;
   return l;
 }
@@ -279,6 +280,7 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
   uint32_t* sres = reinterpret_cast<uint32_t*>(w + lay.sres);
   uint32_t* proj = proj_out ? proj_out : reinterpret_cast<uint32_t*>(w + lay.proj);
   float2* norms = reinterpret_cast<float2*>(w + lay.norms);
+  float* seeds = reinterpret_cast<float*>(w + lay.seeds);
   const bool screened = p->screen != PG_SCREEN_NONE && pg::screen_supported(L, d, 1);
   unsigned long long* cnt = h->d_counters;
   const int sms = h->num_sms;
@@ -385,6 +387,9 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
       sa.seg_count = seg_count;
       sa.rows = h->tune.search_rows;
       sa.max_blocks_per_sm = h->tune.search_warps_per_sm;
+      // the queries (the base points) and their seeds are the same in every round
+      if (r == 0) PG_CUDA(pg::launch_seed_dists(sa, seeds, sms, s));
+      sa.seed_dist = seeds;
       PG_CUDA(pg::launch_search(sa, sms, h->smem_optin, s));
       if (stage_events) PG_CUDA(cudaEventRecord(h->ev[2 + 3 * r], s));
       PG_CUDA(cudaMemsetAsync(indeg, 0, n * 4, s));

@@ -82,6 +82,9 @@ struct SearchArgs {
   // kernel) and a cap on resident search warps per SM; 0 = defaults
   uint32_t rows;
   uint32_t max_blocks_per_sm;
+  // optional (n or nq) x 32: each query's distances to its 32 seeds from launch_seed_dists (the
+  // same values the search would compute); NULL = the search scores the seeds itself
+  const float* seed_dist;
 };
 
 // CPU RoarGraph path on the GPU (tests/test_t2iend.cu:365-613), pg_roar.cu.
@@ -171,6 +174,8 @@ cudaError_t launch_merge_prune(const MergeArgs& a, int num_sms, cudaStream_t st)
 // Returns cudaErrorInvalidValue for parameter combinations the search kernel was not built for
 // (see search_supported).
 cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, cudaStream_t st);
+// Every query's 32 seed distances in the search's FP32 order into out (queries x 32).
+cudaError_t launch_seed_dists(const SearchArgs& a, float* out, int num_sms, cudaStream_t st);
 bool search_supported(uint32_t d, uint32_t km, uint32_t kp, uint32_t kd);
 // Screened (FP16 or BF16 tensor-core Gram + exact re-scoring) prune for strict rounds,
 // c <= 96, 4 <= d <= 1024, d % 4 == 0.

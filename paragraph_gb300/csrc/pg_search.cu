@@ -306,8 +306,13 @@ __global__ void __launch_bounds__(32, KSTEPS <= 8 ? 20 : 12) k_search_m32(Search
       }
       const uint32_t node =
           static_cast<uint32_t>((a.seed_base + static_cast<uint64_t>(lane)) % sn + soff);
-      const float dist = score_passes<KSTEPS, ROWS>(a, q, node, true, rows, mbar, phase, ok);
-      if (!ok) break;
+      float dist;
+      if (a.seed_dist) {  // scored for every query at once by k_seed_dists
+        dist = a.seed_dist[static_cast<uint64_t>(qid) * 32u + lane];
+      } else {
+        dist = score_passes<KSTEPS, ROWS>(a, q, node, true, rows, mbar, phase, ok);
+        if (!ok) break;
+      }
       cand_key = pack_key(dist, 32u + lane);
       cand_id = node;
       ev += (lane == 0) ? 32u : 0u;
@@ -487,8 +492,13 @@ __global__ void __launch_bounds__(32, KSTEPS <= 8 ? 16 : 8) k_search_mk(SearchAr
       }
       const uint32_t node =
           static_cast<uint32_t>((a.seed_base + static_cast<uint64_t>(lane)) % sn + soff);
-      const float dist = score_passes<KSTEPS, ROWS>(a, q, node, true, rows, mbar, phase, ok);
-      if (!ok) break;
+      float dist;
+      if (a.seed_dist) {
+        dist = a.seed_dist[static_cast<uint64_t>(qid) * 32u + lane];
+      } else {
+        dist = score_passes<KSTEPS, ROWS>(a, q, node, true, rows, mbar, phase, ok);
+        if (!ok) break;
+      }
       cand_key = pack_key(dist, KM + lane);
       cand_id = node;
       ev += (lane == 0) ? 32u : 0u;
@@ -718,6 +728,64 @@ static cudaError_t launch_search_m32(const SearchArgs& a, int num_sms, size_t sm
   const uint64_t nq = a.queries ? a.nq : a.n;
   if (blocks > nq) blocks = nq;
   kern<<<static_cast<unsigned>(blocks), 32, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+// The distances of every query to its 32 seeds ((seed_base + s) % n_sub + offset), in the
+// search's FP32 order (Gsearcher.cuh:958-976): residue r = i mod 32 accumulates q[i]*x[i] in i
+// order, then the shuffle-down tree 16, 8, 4, 2, 1.  Lane s holds seed s's 32 residue chains in
+// registers and folds them in the tree's pairs.  The seeds of one (sub-)index are the same 32
+// rows for every query, so they stay in L1; this pass replaces the four staging passes per query
+// and round that scoring the seeds inside the search takes.  One warp per query.
+__global__ void __launch_bounds__(256) k_seed_dists(SearchArgs a, float* __restrict__ out) {
+  const uint32_t lane = lane_id();
+  const uint64_t nq = a.queries ? a.nq : a.n;
+  const uint64_t nw = static_cast<uint64_t>(gridDim.x) * (blockDim.x >> 5);
+  const uint32_t d = a.d;
+  for (uint64_t qid = blockIdx.x * static_cast<uint64_t>(blockDim.x >> 5) + (threadIdx.x >> 5);
+       qid < nq; qid += nw) {
+    uint64_t soff = 0, sn = a.n;
+    if (a.seg_count) {
+      const uint32_t sg = segment_of(a.seg_off, a.seg_count, qid);
+      soff = a.seg_off[sg];
+      sn = a.seg_off[sg + 1] - soff;
+    }
+    const uint64_t node = (a.seed_base + static_cast<uint64_t>(lane)) % sn + soff;
+    const float4* q4 =
+        reinterpret_cast<const float4*>((a.queries ? a.queries : a.base) + qid * d);
+    const float4* x4 = reinterpret_cast<const float4*>(a.base + node * d);
+    float s[32];
+#pragma unroll
+    for (int r = 0; r < 32; r++) s[r] = 0.f;
+    for (uint32_t b = 0; b < d; b += 32) {
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        if (b + 4u * j < d) {
+          const float4 q = __ldg(q4 + (b >> 2) + j);
+          const float4 x = __ldg(x4 + (b >> 2) + j);
+          s[4 * j] = fmaf(q.x, x.x, s[4 * j]);
+          s[4 * j + 1] = fmaf(q.y, x.y, s[4 * j + 1]);
+          s[4 * j + 2] = fmaf(q.z, x.z, s[4 * j + 2]);
+          s[4 * j + 3] = fmaf(q.w, x.w, s[4 * j + 3]);
+        }
+      }
+    }
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1)
+#pragma unroll
+      for (int r = 0; r < w; r++) s[r] = s[r] + s[r + w];
+    out[qid * 32u + lane] = -s[0];
+  }
+}
+
+cudaError_t launch_seed_dists(const SearchArgs& a, float* out, int num_sms, cudaStream_t st) {
+  if (a.d == 0 || (a.d % 4) != 0 || !out) return cudaErrorInvalidValue;
+  const uint64_t nq = a.queries ? a.nq : a.n;
+  if (nq == 0) return cudaSuccess;
+  uint64_t blocks = (nq + 7) / 8;
+  const uint64_t cap = static_cast<uint64_t>(num_sms) * 8;
+  if (blocks > cap) blocks = cap;
+  k_seed_dists<<<static_cast<unsigned>(blocks), 256, 0, st>>>(a, out);
   return cudaGetLastError();
 }
 
