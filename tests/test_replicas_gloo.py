@@ -53,3 +53,16 @@ def test_reference_arm_under_torchrun_prints_once():
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port"
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["ms_per_step"] is not None and line["ms_per_step"] > 0  # the whole build fit
+
+
+def test_metric_names():
+    """The default workload's metric string, and the batched form naming its sub-indexes."""
+    sys.path.insert(0, ROOT)
+    import argparse
+    import bench
+    a = argparse.Namespace(n=1_000_000, d=200, degree=32, beam=64, cosine=False, batched=0)
+    assert bench.metric_name(a) == ("distance_evals_per_s (build, 1Mx200 IP, M=32, L=64, "
+                                    "screened vs FP32, identical edges)")
+    a = argparse.Namespace(n=1_000_000, d=512, degree=32, beam=64, cosine=False, batched=64)
+    assert "64 sub-indexes, 9769080x512" in bench.metric_name(a, 9769080)
