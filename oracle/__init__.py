@@ -4,9 +4,11 @@ The restatement lives in ``pg_oracle.c`` (built to ``_build/libpg_oracle.so`` by
 ``build_oracle.sh``).  Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU legs
 import this module; the ``paragraph_gb300`` package never does.
 
-``ref_harness`` wraps ``_ref/libref_harness_<N>_<D>.so``: the reference's own thread-per-node
-kernels (include/Gbuilder.cuh) compiled with g++ and run on one CPU thread.  It exists only where
-the reference tree was available at build time and is used to make the golden fixtures.
+``RefHarness`` wraps ``_ref/libref_harness_<N>_<D>.so``: the reference's own thread-per-node
+kernels (include/Gbuilder.cuh) compiled with g++ and run on one CPU thread.  ``RefSearchHarness``
+wraps ``_ref/libref_search.so``: the reference's warp-per-query beam searches
+(include/Gsearcher.cuh) under a 32-lane warp emulator.  Both exist only where the reference tree
+was available at build time and are used to make the golden fixtures.
 """
 from __future__ import annotations
 
@@ -294,6 +296,61 @@ class RefHarness:
         self.L.ref_hash_sequence(_p(keys, _u32p), rb.ctypes.data_as(u8p), len(keys),
                                  out.ctypes.data_as(u8p))
         return out
+
+
+class RefSearchHarness:
+    """The reference's own beam-search kernels under a 32-lane warp emulator (see
+    ref_search_harness.cpp): link_process_v0_store_base_data (Gsearcher.cuh:890-1066) at the
+    compiled size n x d, and search_shared_hashtable (Gsearcher.cuh:108-296) at its own compiled
+    shape."""
+
+    def __init__(self, path: str):
+        L = ctypes.CDLL(path)
+        L.ref_search_n.restype = ctypes.c_uint32
+        L.ref_search_d.restype = ctypes.c_uint32
+        L.ref_search_error.restype = ctypes.c_char_p
+        L.ref_link_search.argtypes = [ctypes.c_uint32, _f32p, _u32p, _u32p, _u64p, _u64p]
+        L.ref_query_shape.argtypes = [_u32p]
+        L.ref_query_search.argtypes = [_f32p, _u32p, _f32p, _u32p, _u64p, _u64p]
+        self.L = L
+        self.n = int(L.ref_search_n())
+        self.d = int(L.ref_search_d())
+        shape = np.zeros(5, dtype=np.uint32)
+        L.ref_query_shape(_p(shape, _u32p))
+        self.query_shape = dict(zip(("n", "d", "nq", "degree", "topk"), map(int, shape)))
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(f"reference search failed ({rc}): "
+                               f"{self.L.ref_search_error().decode()}")
+
+    def link_search(self, base, graph):
+        """Returns (ids n x 64, evals per query, iterations per query)."""
+        base = _f32(base)
+        graph = _u32(graph)
+        assert base.shape == (self.n, self.d) and graph.shape[0] == self.n
+        out = np.empty((self.n, 64), dtype=np.uint32)
+        ev = np.zeros(self.n, dtype=np.uint64)
+        it = np.zeros(self.n, dtype=np.uint64)
+        self._check(self.L.ref_link_search(graph.shape[1], _p(base, _f32p), _p(graph, _u32p),
+                                           _p(out, _u32p), _p(ev, _u64p), _p(it, _u64p)))
+        return out, ev, it
+
+    def query_search(self, base, graph, queries):
+        """Returns (ids nq x topk, evals per query, iterations per query)."""
+        s = self.query_shape
+        base = _f32(base)
+        graph = _u32(graph)
+        queries = _f32(queries)
+        assert base.shape == (s["n"], s["d"]) and graph.shape == (s["n"], s["degree"])
+        assert queries.shape == (s["nq"], s["d"])
+        out = np.empty((s["nq"], s["topk"]), dtype=np.uint32)
+        ev = np.zeros(s["nq"], dtype=np.uint64)
+        it = np.zeros(s["nq"], dtype=np.uint64)
+        self._check(self.L.ref_query_search(_p(base, _f32p), _p(graph, _u32p),
+                                            _p(queries, _f32p), _p(out, _u32p), _p(ev, _u64p),
+                                            _p(it, _u64p)))
+        return out, ev, it
 
 
 def split_lists(lists: np.ndarray, r: int, p: int):

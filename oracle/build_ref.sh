@@ -5,7 +5,7 @@
 # oracle/_ref/ (git-ignored).  Usage: oracle/build_ref.sh [REFERENCE_ROOT] [N] [D]
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${1:-/root/reference}"
+ref="${1:-${PG_REFERENCE_ROOT:-$(dirname "$(dirname "$here")")/reference}}"
 n="${2:-1000}"
 d="${3:-200}"
 if [ ! -f "$ref/include/Gbuilder.cuh" ]; then

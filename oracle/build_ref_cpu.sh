@@ -4,9 +4,11 @@
 # oracle/ref_cpu_harness.cu.  x86-64 with AVX-512 only (the reference's compare is AVX-512 code).
 # Test infrastructure only; the output stays in oracle/_ref/ (git-ignored).
 # Usage: oracle/build_ref_cpu.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT defaults to $PG_REFERENCE_ROOT, else the checkout named "reference" beside
+#   this repository.
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${1:-/root/reference}"
+ref="${1:-${PG_REFERENCE_ROOT:-$(dirname "$(dirname "$here")")/reference}}"
 if [ ! -f "$ref/tests/test_t2iend.cu" ]; then
   echo "reference tree not found at $ref" >&2
   exit 2

@@ -2,7 +2,9 @@
 
 Every comparison is bit-exact on ids (integer work).  The stage tests feed each kernel the exact
 inputs the reference kernels received (tests/golden/ref_*.npz, produced by the reference's own
-code) and compare every output; the search and whole-build tests compare against the oracle.
+code) and compare every output; the search is compared with the reference's own search kernel
+run under a warp emulator (tests/golden/ref_search_*.npz) and with the oracle; the whole-build
+tests compare against the oracle.
 """
 import os
 
@@ -121,6 +123,25 @@ def test_search_matches_oracle(handle, golden_dir, case):
     assert np.array_equal(got, ref), f"{(got != ref).any(axis=1).sum()} rows differ"
     assert (ev, it) == (rev, rit)
     assert np.array_equal(got, f["search_in"])
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("graph", ["proj", "link32_graph", "link55_graph"])
+def test_search_matches_reference_search(handle, golden_dir, case, graph):
+    """k_search_m32 against the reference's own link_process_v0_store_base_data
+    (Gsearcher.cuh:890-1066), run under the warp emulator on the same inputs
+    (tests/golden/ref_search_*.npz): the round-1 search over the projection and the round-2
+    search over the reference-merged link graphs, id for id, with the evaluation and iteration
+    counts."""
+    f = load(golden_dir, case)
+    r = np.load(os.path.join(golden_dir, f"ref_search_{case}_1000x200.npz"))
+    out = empty_u32(1000, 64)
+    ev, it = handle.search(dev_f32(f["base"]), dev_u32(f[graph]), out)
+    got = host_u32(out)
+    want = r[f"{graph}_ids"]
+    assert np.array_equal(got, want), f"{(got != want).any(axis=1).sum()} rows differ"
+    assert ev == int(r[f"{graph}_evals"].sum())
+    assert it == int(r[f"{graph}_iters"].sum())
 
 
 @pytest.mark.parametrize("km", [32, 64])

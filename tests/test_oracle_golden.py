@@ -1,8 +1,11 @@
 """The oracle against the reference's own kernels (CPU, no GPU needed).
 
 tests/golden/ref_*.npz hold the outputs of the reference's thread-per-node kernels
-(include/Gbuilder.cuh) run on one thread by tests/golden/make_golden.py.  The oracle must
-reproduce every stage bit for bit: this pins oracle/pg_oracle.c to the reference.
+(include/Gbuilder.cuh) run on one thread by tests/golden/make_golden.py;
+tests/golden/ref_search_*.npz and ref_qsearch_*.npz those of its warp-per-query beam searches
+(include/Gsearcher.cuh) run under a 32-lane warp emulator by tests/golden/make_golden_search.py.
+The oracle must reproduce every stage bit for bit: this pins oracle/pg_oracle.c to the
+reference.
 """
 import numpy as np
 import pytest
@@ -108,3 +111,43 @@ def test_full_build_runs_and_is_deterministic(golden_dir):
     assert (g[valid] < n).all()
     assert not (g == np.arange(n, dtype=np.uint32)[:, None]).any(), "no self loops"
     assert a["stats"]["evals_total"] > 0 and not a["stats"]["cap_hit"]
+
+
+SEARCH_GRAPHS = ["proj", "link32_graph", "link55_graph"]
+
+
+@pytest.mark.parametrize("case", ["mix", "edge"])
+@pytest.mark.parametrize("graph", SEARCH_GRAPHS)
+def test_search_matches_reference_search(golden_dir, case, graph):
+    """The oracle's beam search against the reference's own link_process_v0_store_base_data
+    (Gsearcher.cuh:890-1066) run under the warp emulator (tests/golden/ref_search_*.npz): every
+    id of every list, and the evaluation and iteration counts."""
+    import os
+    f = load(golden_dir, case)
+    r = np.load(os.path.join(golden_dir, f"ref_search_{case}_1000x200.npz"))
+    ids, ev, it, hit = oracle.search(f["base"], f[graph])
+    assert not hit
+    assert np.array_equal(ids, r[f"{graph}_ids"]), f"{(ids != r[graph + '_ids']).any(1).sum()} rows"
+    assert ev == int(r[f"{graph}_evals"].sum())
+    assert it == int(r[f"{graph}_iters"].sum())
+
+
+def test_search_fixture_is_the_link_rounds_input(golden_dir):
+    """The round-1 search input of the stage fixtures (search_in) is the reference search's own
+    output over the reference-made projection."""
+    import os
+    for case in ("mix", "edge"):
+        f = load(golden_dir, case)
+        r = np.load(os.path.join(golden_dir, f"ref_search_{case}_1000x200.npz"))
+        assert np.array_equal(f["search_in"], r["proj_ids"])
+
+
+def test_query_search_matches_reference(golden_dir):
+    """The oracle's query search against the reference's search_shared_hashtable
+    (Gsearcher.cuh:108-296) under the warp emulator: 300 cross-modal queries, topk 10."""
+    import os
+    q = np.load(os.path.join(golden_dir, "ref_qsearch_2000x64.npz"))
+    ids, ev, it = oracle.query_search(q["base"], q["graph"], q["queries"], topk=int(q["topk"]),
+                                      reset_iter=int(q["reset_iter"]))
+    assert np.array_equal(ids, q["ids"])
+    assert (ev, it) == (int(q["evals"].sum()), int(q["iters"].sum()))

@@ -1,5 +1,8 @@
 """Query-time search (search_shared_hashtable, Gsearcher.cuh:108-296) over a built graph.
 
+The reference's own kernel, run under a warp emulator, pins both the oracle
+(test_oracle_golden.py) and pg_query_search (below) on tests/golden/ref_qsearch_2000x64.npz.
+
 CPU: the oracle's query search, given base rows as the queries, returns the first ids of the
 build-time search rows (the same walk, output cut to topk).  GPU: pg_query_search returns the
 oracle's ids bit for bit on held-out cross-modal queries, and recall@10 against exact
@@ -67,3 +70,28 @@ def test_gpu_query_search_equals_oracle(data, km):
     assert np.array_equal(ids, ref)
     assert (ev, it) == (ev_ref, it_ref)
     print(f"GPU recall@10 L={km + 32}: {recall_at(ids, truth):.4f}")
+
+
+@pytest.mark.gpu
+def test_gpu_query_search_equals_reference(golden_dir):
+    """pg_query_search against the reference's own search_shared_hashtable
+    (Gsearcher.cuh:108-296) run under the warp emulator (tests/golden/ref_qsearch_2000x64.npz):
+    300 cross-modal queries over a degree-32 graph, id for id, with evaluation and iteration
+    counts."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import os
+
+    import paragraph_gb300 as pg
+    q = np.load(os.path.join(golden_dir, "ref_qsearch_2000x64.npz"))
+    nq, topk = q["queries"].shape[0], int(q["topk"])
+    out = torch.full((nq, topk), -1, dtype=torch.int32, device="cuda")
+    with pg.Handle(0) as h:
+        ev, it = h.query_search(torch.from_numpy(q["base"]).cuda(),
+                                torch.from_numpy(q["graph"].view(np.int32)).cuda(),
+                                torch.from_numpy(q["queries"]).cuda(), out,
+                                reset_iter=int(q["reset_iter"]))
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), q["ids"])
+    assert (ev, it) == (int(q["evals"].sum()), int(q["iters"].sum()))
