@@ -180,32 +180,52 @@ def gpu_workload(args, device, queries: bool = False):
                                      centers=args.centers)
 
 
+# DRAM bytes (read + write) per launch of the search kernel on the default workload
+# (1M x 200 IP, M = 32, L = 64, FP16-screened build), measured by ncu
+# (profiles/k_search_m32_1Mx200_dram.md): round 1 over the projection, round 2 over the link graph.
+SEARCH_DRAM_BYTES = {(1_000_000, 200, 32, 64, False): None}
+
+
 def search_roofline(st, args, peak_gbs, peak_kind, rounds):
     """Dominant kernel = the beam search (K4/K8).  Algorithmic bytes per launch: every counted
-    evaluation gathers one 4*D-byte row plus its 4-byte id, every iteration reads Kp*Kd graph ids,
-    and the launch writes n*L ids and reads each query row once."""
-    L = args.beam
-    tot_bytes = 0.0
-    tot_ms = 0.0
-    for r in range(rounds):
-        ev = st.evals_search[r]
-        it = st.search_iters[r]
-        tot_bytes += ev * (4 * args.d + 4) + it * 32 * 4 + args.n * (L * 4 + 4 * args.d)
-        tot_ms += st.ms_search[r]
-    achieved = tot_bytes / (tot_ms / 1e3) / 1e9
-    traffic = None  # DRAM bytes per launch from the committed ncu summary of this workload
-    tpath = os.path.join(ROOT, "profiles", "kernels_1Mx200_metrics.md")
-    if args.n == 1_000_000 and args.d == 200 and os.path.exists(tpath):
-        for line in open(tpath):
-            if line.startswith("search_dram_bytes_per_launch:"):
-                traffic = int(line.split(":")[1])
-    kname = "k_search_m32" if args.beam <= 32 * 2 else "k_search_mk"
-    return {"kernel": f"{kname} (K4/K8 beam search)", "bound": "hbm",
-            "achieved": round(achieved, 1), "peak": peak_gbs, "peak_kind": peak_kind,
-            "unit": "GB/s", "frac": round(achieved / peak_gbs, 4),
-            "traffic": traffic, "algorithmic_bytes_per_launch": round(tot_bytes / rounds),
-            "note": "algorithmic bytes = gathered rows; L2 serves them (98.9% hits, ~5.7 TB/s of "
-                    "L2 traffic) and DRAM moves `traffic` bytes per launch"}
+    evaluation after the 32 seeds gathers one 4*D-byte row plus its 4-byte id, every iteration
+    reads Kp*Kd = 32 graph ids, and the launch reads each query row and its 32 seed distances once
+    and writes n*L ids.  The seed distances are computed once per build by the seed pre-pass
+    (k_seed_dists, timed inside round 1's stage: it reads the n query rows and writes n*32
+    distances), so no search launch gathers a seed row.  The reported launch is the last round's
+    search, whose stage time is that one kernel."""
+    n, d, L = args.n, args.d, args.beam
+
+    def kernel_bytes(r):
+        gathered = st.evals_search[r] - 32 * n
+        return gathered * (4 * d + 4) + st.search_iters[r] * 32 * 4 + n * (4 * d + 32 * 4 + 4 * L)
+
+    last = rounds - 1
+    by = kernel_bytes(last)
+    ms = st.ms_search[last]
+    if last == 0:  # the stage also holds the seed pre-pass
+        by += n * (4 * d + 32 * 4)
+    achieved = by / (ms / 1e3) / 1e9
+    dram = SEARCH_DRAM_BYTES.get((args.n, args.d, args.degree, args.beam, bool(args.cosine)))
+    traffic = dram[last] if dram else None
+    kname = "k_search_m32" if args.beam - 32 <= 32 else "k_search_mk"
+    out = {"kernel": f"{kname} (round-{last + 1} beam search)",
+           "bound": "latency: L2-resident row gathers, not HBM (see dram_frac)",
+           "achieved": round(achieved, 1), "peak": peak_gbs, "peak_kind": peak_kind,
+           "unit": "GB/s", "frac": round(achieved / peak_gbs, 4),
+           "frac_meaning": "algorithmic gathered bytes / launch time / measured HBM copy peak",
+           "traffic": traffic, "algorithmic_bytes_per_launch": int(by),
+           "ms_per_launch": round(ms, 3)}
+    if traffic:
+        out["dram_gbs"] = round(traffic / (ms / 1e3) / 1e9, 1)
+        out["dram_frac"] = round(traffic / (ms / 1e3) / 1e9 / peak_gbs, 4)
+    if rounds > 1:
+        b0 = kernel_bytes(0) + n * (4 * d + 32 * 4)
+        out["round1_stage"] = {"algorithmic_bytes": int(b0), "ms": round(st.ms_search[0], 3),
+                               "achieved": round(b0 / (st.ms_search[0] / 1e3) / 1e9, 1),
+                               "traffic": dram[0] if dram else None,
+                               "includes": "seed pre-pass + round-1 search"}
+    return out
 
 
 def cpu_baseline_sample(args, base_np, gt_np, seconds):
@@ -242,14 +262,28 @@ def cpu_baseline_sample(args, base_np, gt_np, seconds):
     return ev / (t3 - t0), desc, oracle.num_threads(), None
 
 
+def workload_config(args) -> dict:
+    """The `config` object of both arms: the workload, nothing measured."""
+    kind = "cosine" if args.cosine else "IP"
+    return {"workload": f"ParaGraph build {args.n}x{args.d} {kind}, gt top-128, "
+                        f"M={args.degree}, L={args.beam}",
+            "n": args.n, "d": args.d, "q": args.n, "degree": args.degree, "beam": args.beam,
+            "centers": args.centers, "seed": args.seed,
+            "l2": f"inputs larger than L2 (base {args.n * args.d * 4 / 1e6:.0f} MB, "
+                  f"gt {args.n * 128 * 4 / 1e6:.0f} MB vs 129 MB L2)"}
+
+
 def run_reference(args):
-    """--impl reference: CPU restatement on the host cores (rank 0 only)."""
+    """--impl reference: the CPU restatement of the path (the oracle, all host threads) on rank 0;
+    one step = one complete build (K0..K11) of the workload."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     import numpy as np
     import torch
+
+    import oracle
     if torch.cuda.is_available():
         base, gt = gpu_workload(args, "cuda")
         base_np = base.cpu().numpy()
@@ -258,35 +292,40 @@ def run_reference(args):
         torch.cuda.empty_cache()
     else:
         from paragraph_gb300 import datagen
-        base_np, gt_np = datagen.make_dataset(args.n, args.d, seed=args.seed)
-    vals = []
-    desc = ""
-    threads = 1
-    full_evals = None
+        base_np, gt_np = datagen.make_dataset(args.n, args.d, seed=args.seed, cosine=args.cosine,
+                                              centers=args.centers)
     steps = max(args.steps, 1)
-    per_step = max(min(args.cpu_seconds, 120.0 / (steps + args.warmup)), 3.0)
+    times = []
+    evals = None
     for i in range(args.warmup + steps):
-        v, desc, threads, full = cpu_baseline_sample(args, base_np, gt_np, per_step)
-        if full is not None:
-            full_evals = full["stats"]["evals_total"]
+        t0 = time.perf_counter()
+        full = oracle.build_graph(base_np, gt_np, degree=args.degree, beam=args.beam)
+        dt = time.perf_counter() - t0
+        ev = full["stats"]["evals_total"]
+        assert evals is None or ev == evals, "evaluation count changed between builds"
+        evals = ev
         if i >= args.warmup:
-            vals.append(v)
-    value = statistics.mean(vals)
-    # one full build at the measured rate (the sample is the whole build when it fits the budget)
-    ms_step = round(full_evals / value * 1e3, 1) if full_evals else None
-    line = {"metric": metric_name(args), "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            times.append(dt)
+    t = statistics.mean(times)
+    value = evals / t
+    threads = oracle.num_threads()
+    desc = (f"oracle full build (K0-K11) of all {args.n} points per step: {evals} evals, "
+            f"{t:.2f} s mean over {steps} steps")
+    line = {"metric": metric_name(args), "value": value, "unit": UNIT, "impl": "reference",
+            "n_gpus": world, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": round(t * 1e3, 1), "ms_each": [round(x * 1e3, 1) for x in times],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded mixture-of-Gaussians stand-in for T2I-style data)",
-            "config": {"workload": f"ParaGraph build {args.n}x{args.d} IP, gt top-128, "
-                                   f"M={args.degree}, L={args.beam}",
-                       "n": args.n, "d": args.d, "degree": args.degree, "beam": args.beam},
+            "config": workload_config(args),
+            "evals_per_build": evals,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "note": "the reference's path is GPU-only; its CPU RoarGraph code is x86 AVX-512 and "
-                    "its sources are not on this host, so the CPU restatement (oracle) stands in"}
+            "note": "the reference's build path is GPU-only, and its CPU RoarGraph code is x86 "
+                    "AVX-512 and absent on this Arm host, so the oracle -- the CPU restatement of "
+                    "the path, pinned to the reference's own kernels by the golden fixtures -- "
+                    "stands in"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -421,19 +460,27 @@ def run_ours(args):
             h.build_host_ptr(base_h.data_ptr(), n, d, gt_h.data_ptr(), gt_h.shape[0],
                              graph_h.data_ptr(), proj_h.data_ptr(), params)
         barrier(world)
-        times = []
+        times, h2d, d2h, dev_ms = [], [], [], []
         est = None
         for _ in range(max(1, args.steps)):
             t0 = time.perf_counter()
             est = h.build_host_ptr(base_h.data_ptr(), n, d, gt_h.data_ptr(), gt_h.shape[0],
                                    graph_h.data_ptr(), proj_h.data_ptr(), params)
             times.append(time.perf_counter() - t0)
+            h2d.append(est.ms_h2d)
+            d2h.append(est.ms_d2h)
+            dev_ms.append(est.ms_total)
         t = allmax(statistics.mean(times), world)
         e2e = {"value": est.evals_total * world / t, "unit": UNIT,
                "h2d_bytes_per_step": int(est.h2d_bytes), "d2h_bytes_per_step": int(est.d2h_bytes),
-               "ms_per_step": round(t * 1e3, 2), "ms_each": [round(x * 1e3, 1) for x in times],
-               "ms_h2d": round(est.ms_h2d, 2), "ms_d2h": round(est.ms_d2h, 2),
-               "timing": "wall clock around each pg_build_host call, mean over --steps calls"}
+               "ms_per_step": round(t * 1e3, 2),
+               "ms_median": round(statistics.median(times) * 1e3, 2),
+               "ms_each": [round(x * 1e3, 1) for x in times],
+               "ms_h2d_each": [round(x, 2) for x in h2d],
+               "ms_d2h_each": [round(x, 2) for x in d2h],
+               "ms_build_each": [round(x, 2) for x in dev_ms],
+               "timing": "wall clock around each pg_build_host call, mean over --steps calls; "
+                         "the copies and the build are also timed with CUDA events per call"}
         base_np = base_h.numpy()
         gt_np = gt_h.numpy().view(np.uint32)
     else:
@@ -460,13 +507,9 @@ def run_ours(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32" if args.screen == "none" else "f32+" + args.screen,
                 "data": "synthetic (seeded mixture-of-Gaussians stand-in for T2I-style data)",
-                "config": {"workload": f"ParaGraph build {args.n}x{args.d} IP, gt top-128, "
-                                       f"M={args.degree}, L={args.beam}",
-                           "n": args.n, "d": args.d, "q": args.n, "degree": args.degree,
-                           "beam": args.beam, "parallelism": "replicas" if world > 1 else "single",
-                           "l2": f"inputs larger than L2 (base {n * d * 4 / 1e6:.0f} MB, "
-                                 f"gt {n * 128 * 4 / 1e6:.0f} MB vs 129 MB L2)",
-                           "build_s": round(ms_step / 1e3, 4)},
+                "config": workload_config(args),
+                "parallelism": "replicas" if world > 1 else "single",
+                "build_s": round(ms_step / 1e3, 4),
                 "evals_per_build": evals,
                 "stage_ms": {"proj": round(s.ms_proj, 2),
                              "search": [round(x, 2) for x in list(s.ms_search)[:params.link_rounds]],

@@ -189,6 +189,14 @@ int pg_build_index(pg_handle h, const pg_params* p, const float* d_base, uint64_
                    const uint32_t* d_gt, uint64_t q, uint32_t match_rounds, uint32_t m_nn,
                    uint32_t m_final, uint32_t out_stride, uint32_t* d_out, uint32_t* d_cnt,
                    pg_stats* st);
+/* pg_build_index with host buffers (base n x d f32, gt q x gt_k u32 in; out n x out_stride and
+ * cnt n out): the inputs are copied to the device, the index is built there and copied back
+ * (the reference driver's host-side flow, tests/test_t2iend.cu:850-873,1228-1258).  Row i holds
+ * cnt[i] ids; the slots after them are unspecified. */
+int pg_build_index_host(pg_handle h, const pg_params* p, const float* base, uint64_t n,
+                        uint32_t d, const uint32_t* gt, uint64_t q, uint32_t match_rounds,
+                        uint32_t m_nn, uint32_t m_final, uint32_t out_stride, uint32_t* out,
+                        uint32_t* cnt, pg_stats* st);
 
 /* ---- ground truth (the reference reads it from files made outside its build, README.md:25-31)
  * pg_ground_truth: for each of nq queries (nq x d, device) the k ids of the base rows (n x d)
@@ -259,9 +267,11 @@ int pg_search(pg_handle h, const float* d_base, uint64_t n, uint32_t d, const ui
  * Needs no handle and allocates nothing: the reverse-edge workspace and counters live in a fixed
  * array inside the library's device image (about 4.6 MB, held by every GPU that loads the
  * library until the process exits).  Limits: n <= 32768 and n * pruned <= 1048576, else
- * PG_EINVAL.  Runs on `stream` (a cudaStream_t) and synchronises it before returning.  All calls
- * share the array: calls that overlap on the GPU race and must be serialised by the caller.  The
- * first call on a device looks up the array's device address; make it before any stream capture.
+ * PG_EINVAL.  Runs on `stream` (a cudaStream_t of the current device), copies the evaluation
+ * count and status to the host and synchronises `stream` before returning.  All calls share the
+ * array: calls that overlap on the GPU race and must be serialised by the caller.  The first call
+ * on a device, and the first after that device's context was reset, looks up the array's device
+ * address there; that first call should come before any stream capture on the device.
  * This entry point has no counterpart in the reference. */
 int pg_prune_reverse_noalloc(void* stream, const float* d_base, uint64_t n, uint32_t d,
                              const uint32_t* d_graph, uint32_t c, uint32_t pruned,

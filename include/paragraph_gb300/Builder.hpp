@@ -3,7 +3,8 @@
 // The reference declares this class (include/Builder.hpp:15-35) but ships it commented out, and
 // src/Builder.cpp is empty; its driver launches the kernel templates directly
 // (tests/test_t2iend.cu:974-1139).  This restores the declared interface -- construction from
-// base vectors and ground-truth ids, SetGt, LaunchBuild -- on top of libparagraph_gb300.so, with
+// base vectors and ground-truth ids, SetGt, LaunchBuild -- on top of libparagraph_gb300.so, adds
+// LaunchIndex for the driver's whole index (the file the driver saves), with
 // sizes as runtime values.  LaunchBuild's template arguments are kept for source compatibility:
 // grid_size/block_size are ignored (the library chooses launch shapes), gt_num and dim are
 // checked against the data.  Errors throw Gbuilder::BuildError carrying the pg_status code.
@@ -58,6 +59,8 @@ class Builder {
         params_(other.params_),
         graph_(std::move(other.graph_)),
         projection_(std::move(other.projection_)),
+        index_(std::move(other.index_)),
+        index_stride_(other.index_stride_),
         stats_(other.stats_),
         ep_(other.ep_) {}
   Builder(Builder& other) = delete;
@@ -81,6 +84,8 @@ class Builder {
     const uint64_t q = gt_ids_.size() / params_.gt_k;
     graph_.assign(n * params_.degree, PG_TOMB);
     projection_.assign(n * params_.proj_degree, PG_TOMB);
+    index_.clear();
+    index_stride_ = 0;
     pg_handle h = nullptr;
     check(pg_create(&h, device_, nullptr));
     const int rc = pg_build_host(h, &params_, reinterpret_cast<const float*>(base_.data()), n,
@@ -91,10 +96,43 @@ class Builder {
     check(pg_entry_point(gt_ids_.data(), q, params_.gt_k, n, &ep_));
   }
 
+  // The reference driver's whole index (tests/test_t2iend.cu:974-1258): the GPU build, then
+  // `match_rounds` MatchSup rounds, FusionNN(m_nn) and FusionFinal(m_final), on the GPU
+  // (pg_build_index_host).  The driver's values are 6, 40 and 70.  The result is index() (n rows
+  // of 2*m_nn + m_final slots, tomb padded), which SaveGraph then writes, as the driver saves its
+  // FusionFinal graph.
+  auto LaunchIndex(uint32_t match_rounds = 6, uint32_t m_nn = 40, uint32_t m_final = 70) -> void {
+    if (dim_ == 0 || base_.size() % dim_ != 0) throw BuildError(PG_EINVAL, "base size % dim");
+    if (gt_ids_.size() % params_.gt_k != 0) throw BuildError(PG_EINVAL, "gt size % gt_k");
+    const uint64_t n = base_.size() / dim_;
+    const uint64_t q = gt_ids_.size() / params_.gt_k;
+    const uint32_t stride = 2 * m_nn + m_final;
+    std::vector<id_type> rows(n * stride);
+    std::vector<uint32_t> cnt(n);
+    pg_handle h = nullptr;
+    check(pg_create(&h, device_, nullptr));
+    const int rc = pg_build_index_host(h, &params_, reinterpret_cast<const float*>(base_.data()),
+                                       n, dim_, gt_ids_.data(), q, match_rounds, m_nn, m_final,
+                                       stride, rows.data(), cnt.data(), &stats_);
+    pg_destroy(h);
+    check(rc);
+    for (uint64_t i = 0; i < n; i++)
+      for (uint32_t j = cnt[i]; j < stride; j++) rows[i * stride + j] = PG_TOMB;
+    index_ = std::move(rows);
+    index_stride_ = stride;
+    check(pg_entry_point(gt_ids_.data(), q, params_.gt_k, n, &ep_));
+  }
+
   auto SetGt(std::vector<id_type>&& gt_ids) -> void { gt_ids_ = std::move(gt_ids); }
 
-  // SaveGraph (tests/test_t2iend.cu:615-633) of the built graph.
+  // SaveGraph (tests/test_t2iend.cu:615-633): the FusionFinal index when LaunchIndex has run
+  // (what the reference driver saves, :1258), else the graph of LaunchBuild.
   auto SaveGraph(std::string const& path) const -> void {
+    if (index_stride_) {
+      check(pg_save_graph(path.c_str(), index_.data(), index_.size() / index_stride_,
+                          index_stride_, ep_));
+      return;
+    }
     check(pg_save_graph(path.c_str(), graph_.data(), graph_.size() / params_.degree,
                         params_.degree, ep_));
   }
@@ -102,6 +140,8 @@ class Builder {
   pg_params& params() { return params_; }
   std::vector<id_type> const& graph() const { return graph_; }
   std::vector<id_type> const& projection() const { return projection_; }
+  std::vector<id_type> const& index() const { return index_; }
+  uint32_t index_stride() const { return index_stride_; }
   pg_stats const& stats() const { return stats_; }
   id_type ep() const { return ep_; }
 
@@ -113,6 +153,8 @@ class Builder {
   pg_params params_{};
   std::vector<id_type> graph_;
   std::vector<id_type> projection_;
+  std::vector<id_type> index_;
+  uint32_t index_stride_ = 0;
   pg_stats stats_{};
   id_type ep_ = 0;
 };

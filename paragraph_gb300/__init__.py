@@ -121,6 +121,9 @@ SIGNATURES = {
                                        _U32, _U32, _U32, _VP, _VP]),
     "pg_build_index": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _U64, _U32, _VP, _U64,
                                       _U32, _U32, _U32, _U32, _VP, _VP, ctypes.POINTER(Stats)]),
+    "pg_build_index_host": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _U64, _U32, _VP,
+                                           _U64, _U32, _U32, _U32, _U32, _VP, _VP,
+                                           ctypes.POINTER(Stats)]),
     "pg_ground_truth": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _U64, _U32, _VP]),
     "pg_set_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
     "pg_get_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
@@ -338,6 +341,25 @@ class Handle:
                                     _ptr(out), _ptr(cnt), ctypes.byref(st)))
         return st
 
+    def build_index_host(self, base: np.ndarray, gt: np.ndarray, params: Params | None = None,
+                         match_rounds: int = 6, m_nn: int = 40, m_final: int = 70):
+        """pg_build_index_host: the whole index from host arrays.  Returns (rows n x
+        (2*m_nn + m_final) tomb padded, counts n, Stats)."""
+        params = params or default_params()
+        base = np.ascontiguousarray(base, dtype=np.float32)
+        gt = np.ascontiguousarray(gt, dtype=np.uint32)
+        n, d = base.shape
+        stride = 2 * m_nn + m_final
+        out = np.empty((n, stride), dtype=np.uint32)
+        cnt = np.empty(n, dtype=np.uint32)
+        st = Stats()
+        _check(lib().pg_build_index_host(self._h, ctypes.byref(params), base.ctypes.data, n, d,
+                                         gt.ctypes.data, gt.shape[0], match_rounds, m_nn,
+                                         m_final, stride, out.ctypes.data, cnt.ctypes.data,
+                                         ctypes.byref(st)))
+        out[np.arange(stride)[None, :] >= cnt[:, None].astype(np.int64)] = TOMB
+        return out, cnt, st
+
     def ground_truth(self, base, queries, out):
         """pg_ground_truth: exact inner-product top-k (k = out.shape[1]) of every query."""
         n, d = base.shape
@@ -442,6 +464,7 @@ class Builder:
         self.device = device
         self.graph = None
         self.projection = None
+        self.index = None
         self.stats = None
         self.ep = None
 
@@ -457,10 +480,24 @@ class Builder:
         with Handle(self.device, stream=0) as h:
             self.graph, self.projection, self.stats = h.build_host(self.base_, self.gt_ids_,
                                                                    self.params)
+        self.index = None
         self.ep = entry_point(self.gt_ids_, self.base_.shape[0])
         return self.graph
 
+    def LaunchIndex(self, match_rounds: int = 6, m_nn: int = 40, m_final: int = 70) -> np.ndarray:
+        """The reference driver's whole index (tests/test_t2iend.cu:974-1258): the build, then
+        MatchSup rounds, FusionNN and FusionFinal; returns the tomb-padded index rows, which
+        SaveGraph then writes (the file the driver saves)."""
+        with Handle(self.device, stream=0) as h:
+            self.index, _, self.stats = h.build_index_host(self.base_, self.gt_ids_, self.params,
+                                                           match_rounds, m_nn, m_final)
+        self.ep = entry_point(self.gt_ids_, self.base_.shape[0])
+        return self.index
+
     def SaveGraph(self, path: str):
-        if self.graph is None:
-            raise PGError(PG_EINVAL, "LaunchBuild has not run")
-        save_graph(path, self.graph, self.ep)
+        """SaveGraph (tests/test_t2iend.cu:615-633): the FusionFinal index after LaunchIndex, else
+        the graph of LaunchBuild."""
+        rows = self.index if self.index is not None else self.graph
+        if rows is None:
+            raise PGError(PG_EINVAL, "neither LaunchBuild nor LaunchIndex has run")
+        save_graph(path, rows, self.ep)

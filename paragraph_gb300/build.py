@@ -1,7 +1,8 @@
 """Builds paragraph_gb300/_lib/libparagraph_gb300.so with nvcc for sm_103a (in-tree).
 
 Each translation unit compiles in its own process (in parallel), then one link step.  The
-library is rebuilt only when a source or header is newer than it.
+library is rebuilt only when a source or header is newer than it, and then only the objects
+older than their source or a shared header are recompiled.
 """
 from __future__ import annotations
 
@@ -49,8 +50,16 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     extra = list(extra or [])
     objs = []
 
+    common = [os.path.join(CSRC, f) for f in HEADERS]
+    common += [os.path.join(ROOT, "include", "paragraph_gb300.h"), __file__]
+    newest_common = max(os.path.getmtime(p) for p in common if os.path.exists(p))
+
     def compile_one(src):
         obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        if (not force and not extra and os.path.exists(obj)
+                and os.path.getmtime(obj) > max(newest_common,
+                                                os.path.getmtime(os.path.join(CSRC, src)))):
+            return obj  # object newer than its source and every shared header
         cmd = [cc, *ARCH, *FLAGS, *extra, "-I", os.path.join(ROOT, "include"), "-c",
                os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -146,6 +146,7 @@ struct pg_handle_s {
   size_t ws2_bytes = 0;
   cudaStream_t copy_stream = nullptr;  // pg_build_host: second host->device copy beside `stream`
   cudaEvent_t copy_done = nullptr;
+  cudaEvent_t host_ev[4] = {};  // pg_build_host: H2D start/end, D2H start/end (made once)
   std::mutex mu;
 };
 
@@ -253,6 +254,12 @@ int status_to_error(uint32_t s) {
   if (s) return fail(PG_ECUDA, "device status 0x%x", s);
   return PG_OK;
 }
+
+}  // namespace
+
+int pg::status_error(uint32_t status) { return status_to_error(status); }
+
+namespace {
 
 // seg_off / qseg_off (host arrays, seg_count + 1 entries each): batched builds only.
 int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, uint32_t d,
@@ -775,6 +782,8 @@ int pg_destroy(pg_handle h) {
   for (int i = 0; i < 16; i++)
     if (h->ev[i]) cudaEventDestroy(h->ev[i]);
   if (h->copy_done) cudaEventDestroy(h->copy_done);
+  for (cudaEvent_t& e : h->host_ev)
+    if (e) cudaEventDestroy(e);
   if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   delete h;
   return PG_OK;
@@ -823,11 +832,9 @@ int pg_build_host(pg_handle h, const pg_params* p, const float* base, uint64_t n
   uint32_t* d_graph = reinterpret_cast<uint32_t*>(h->inbuf + bb + gb);
   uint32_t* d_proj = reinterpret_cast<uint32_t*>(h->inbuf + bb + gb + ob);
   cudaStream_t s = h->stream;
-  cudaEvent_t t0, t1, t2, t3;
-  PG_CUDA(cudaEventCreate(&t0));
-  PG_CUDA(cudaEventCreate(&t1));
-  PG_CUDA(cudaEventCreate(&t2));
-  PG_CUDA(cudaEventCreate(&t3));
+  for (cudaEvent_t& e : h->host_ev)
+    if (!e) PG_CUDA(cudaEventCreate(&e));
+  cudaEvent_t t0 = h->host_ev[0], t1 = h->host_ev[1], t2 = h->host_ev[2], t3 = h->host_ev[3];
   if (!h->copy_stream) {
     PG_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
     PG_CUDA(cudaEventCreateWithFlags(&h->copy_done, cudaEventDisableTiming));
@@ -849,13 +856,7 @@ int pg_build_host(pg_handle h, const pg_params* p, const float* base, uint64_t n
   PG_CUDA(cudaEventRecord(t1, s));
   if (st) std::memset(st, 0, sizeof(*st));
   rc = run_build(h, p, d_base, n, d, d_gt, q, d_graph, d_proj, st);
-  if (rc) {
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
-    cudaEventDestroy(t2);
-    cudaEventDestroy(t3);
-    return rc;
-  }
+  if (rc) return rc;
   PG_CUDA(cudaEventRecord(t2, s));
   uint64_t d2h = 0;
   if (graph && p->link_rounds > 0) {
@@ -874,10 +875,6 @@ int pg_build_host(pg_handle h, const pg_params* p, const float* base, uint64_t n
     st->h2d_bytes = n * d * 4 + q * p->gt_k * 4;
     st->d2h_bytes = d2h;
   }
-  cudaEventDestroy(t0);
-  cudaEventDestroy(t1);
-  cudaEventDestroy(t2);
-  cudaEventDestroy(t3);
   return PG_OK;
 }
 
@@ -1357,15 +1354,15 @@ int pg_fusion_final(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
   return finish(h);
 }
 
-int pg_build_index(pg_handle h, const pg_params* p, const float* d_base, uint64_t n, uint32_t d,
-                   const uint32_t* d_gt, uint64_t q, uint32_t match_rounds, uint32_t m_nn,
-                   uint32_t m_final, uint32_t out_stride, uint32_t* d_out, uint32_t* d_cnt,
-                   pg_stats* st) {
+namespace {
+
+// Argument checks shared by pg_build_index and pg_build_index_host.
+int check_index(pg_handle h, const pg_params* p, uint64_t n, uint32_t d, uint64_t q,
+                uint32_t match_rounds, uint32_t m_nn, uint32_t m_final, uint32_t out_stride) {
   if (!h) return fail(PG_EINVAL, "handle is NULL");
   int rc = check_params(p, n, d, q);
   if (rc) return rc;
   if (p->link_rounds == 0) return fail(PG_EINVAL, "the index needs the link graph (link_rounds > 0)");
-  if (!d_base || !d_gt || !d_out || !d_cnt) return fail(PG_EINVAL, "NULL argument");
   if (match_rounds < 1 || match_rounds >= p->gt_k)
     return fail(PG_EINVAL, "match_rounds must be in [1, gt_k)");
   rc = check_sup(n, d, q, p->gt_k, match_rounds, m_nn);
@@ -1377,9 +1374,15 @@ int pg_build_index(pg_handle h, const pg_params* p, const float* d_base, uint64_
   if (m_final < 1 || m_final > 128) return fail(PG_EINVAL, "m_final must be in [1, 128]");
   if (out_stride < 2 * m_nn + m_final)
     return fail(PG_EINVAL, "out_stride must be >= 2*m_nn + m_final = %u", 2 * m_nn + m_final);
-  if (!aligned16(d_base)) return fail(PG_EINVAL, "base must be 16-byte aligned");
-  std::lock_guard<std::mutex> lk(h->mu);
-  PG_CUDA(cudaSetDevice(h->device));
+  return PG_OK;
+}
+
+// The whole index on device buffers; the caller holds h->mu with h->device current.
+int build_index_locked(pg_handle h, const pg_params* p, const float* d_base, uint64_t n,
+                       uint32_t d, const uint32_t* d_gt, uint64_t q, uint32_t match_rounds,
+                       uint32_t m_nn, uint32_t m_final, uint32_t out_stride, uint32_t* d_out,
+                       uint32_t* d_cnt, pg_stats* st) {
+  int rc = PG_OK;
   if (st) std::memset(st, 0, sizeof(*st));
   // graphs that outlive a stage: link graph, projection, the rounds' lists, FusionNN's lists
   const size_t b_link = align_up(n * p->degree * 4), b_proj = align_up(n * p->proj_degree * 4);
@@ -1442,6 +1445,52 @@ int pg_build_index(pg_handle h, const pg_params* p, const float* d_base, uint64_
   }
   return PG_OK;
 }
+
+}  // namespace
+
+int pg_build_index(pg_handle h, const pg_params* p, const float* d_base, uint64_t n, uint32_t d,
+                   const uint32_t* d_gt, uint64_t q, uint32_t match_rounds, uint32_t m_nn,
+                   uint32_t m_final, uint32_t out_stride, uint32_t* d_out, uint32_t* d_cnt,
+                   pg_stats* st) {
+  int rc = check_index(h, p, n, d, q, match_rounds, m_nn, m_final, out_stride);
+  if (rc) return rc;
+  if (!d_base || !d_gt || !d_out || !d_cnt) return fail(PG_EINVAL, "NULL argument");
+  if (!aligned16(d_base)) return fail(PG_EINVAL, "base must be 16-byte aligned");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  return build_index_locked(h, p, d_base, n, d, d_gt, q, match_rounds, m_nn, m_final, out_stride,
+                            d_out, d_cnt, st);
+}
+
+int pg_build_index_host(pg_handle h, const pg_params* p, const float* base, uint64_t n,
+                        uint32_t d, const uint32_t* gt, uint64_t q, uint32_t match_rounds,
+                        uint32_t m_nn, uint32_t m_final, uint32_t out_stride, uint32_t* out,
+                        uint32_t* cnt, pg_stats* st) {
+  int rc = check_index(h, p, n, d, q, match_rounds, m_nn, m_final, out_stride);
+  if (rc) return rc;
+  if (!base || !gt || !out || !cnt) return fail(PG_EINVAL, "NULL argument");
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  const size_t bb = align_up(n * d * 4), gb = align_up(q * p->gt_k * 4);
+  const size_t ob = align_up(n * out_stride * 4), cb = align_up(n * 4);
+  rc = ensure_in(h, bb + gb + ob + cb);
+  if (rc) return rc;
+  float* d_base = reinterpret_cast<float*>(h->inbuf);
+  uint32_t* d_gt = reinterpret_cast<uint32_t*>(h->inbuf + bb);
+  uint32_t* d_out = reinterpret_cast<uint32_t*>(h->inbuf + bb + gb);
+  uint32_t* d_cnt = reinterpret_cast<uint32_t*>(h->inbuf + bb + gb + ob);
+  cudaStream_t s = h->stream;
+  PG_CUDA(cudaMemcpyAsync(d_base, base, n * d * 4, cudaMemcpyHostToDevice, s));
+  PG_CUDA(cudaMemcpyAsync(d_gt, gt, q * p->gt_k * 4, cudaMemcpyHostToDevice, s));
+  rc = build_index_locked(h, p, d_base, n, d, d_gt, q, match_rounds, m_nn, m_final, out_stride,
+                          d_out, d_cnt, st);
+  if (rc) return rc;
+  PG_CUDA(cudaMemcpyAsync(out, d_out, n * out_stride * 4, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaMemcpyAsync(cnt, d_cnt, n * 4, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  return PG_OK;
+}
+
 
 // ---------------------------------------------------------------- ground truth
 

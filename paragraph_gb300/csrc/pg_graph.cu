@@ -387,6 +387,8 @@ __global__ void __launch_bounds__(256) k_prune_reverse(PruneArgs a) {
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;
+// callers size the tile-sum buffers by kScanTileElems (pg_kernels.h)
+static_assert(kScanTile == kScanTileElems, "scan tile size must match kScanTileElems");
 
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums,
                                                          uint32_t* total) {

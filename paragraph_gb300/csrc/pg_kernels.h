@@ -190,5 +190,8 @@ constexpr uint32_t kScanTileElems = 4096;
 
 // Records `msg` as the calling thread's pg_last_error() text and returns `code`.
 int set_last_error(int code, const char* msg);
+// Maps a device status word (kErr* bits) to the pg_status and pg_last_error() message every
+// entry point reports.
+int status_error(uint32_t status);
 
 }  // namespace pg

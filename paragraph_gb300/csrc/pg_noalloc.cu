@@ -14,8 +14,11 @@
 // Every call shares the one array, which keeps the previous call's contents: each call clears
 // the parts that must start at zero.  Calls whose work overlaps on the GPU (different streams or
 // threads at the same time) race on the array and must be serialised by the caller.
-// The first call on a device looks up the array's device address there (see scratch_ptr); make
-// that first call before any stream capture.
+// The first call on a device -- and the first after the device's context was reset -- looks up
+// the array's device address there (see scratch_ptr); that first call should come before any
+// stream capture on the device.  `stream` must belong to the current device.
+#include <cuda.h>
+
 #include <cstring>
 #include <mutex>
 
@@ -51,19 +54,57 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_ptr_mu;
 uint32_t* g_ptr[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};  // context the cached address belongs to
 
-// Device address of g_noalloc_scratch on the current device, looked up once per device.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the current device's context (cuCtxGetId, reached through the runtime's driver
+// entry points, so the library needs no link to the driver library).  A reset device gets a new
+// context and so a new id.  Called with g_ptr_mu held.
+cudaError_t current_ctx_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                                     cudaEnableDefault, &q1);
+    if (e != cudaSuccess) return e;
+    e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e != cudaSuccess) return e;
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return cudaErrorSymbolNotFound;
+    get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return cudaErrorDeviceUninitialized;
+  if (get_id(ctx, id) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+  return cudaSuccess;
+}
+
+// Device address of g_noalloc_scratch on the current device.  The lookup runs once per device
+// and again whenever the device's context has changed (a cudaDeviceReset reloads the module, and
+// the array may then sit at another address).
 cudaError_t scratch_ptr(uint32_t** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lk(g_ptr_mu);
-  if (!g_ptr[dev]) {
+  e = cudaSetDevice(dev);  // makes the device's primary context current (initialising it)
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(g_ptr_mu);  // guards the cache and the entry-point lookup
+  unsigned long long ctx = 0;
+  e = current_ctx_id(&ctx);
+  if (e != cudaSuccess) return e;
+  if (!g_ptr[dev] || g_ctx_id[dev] != ctx) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
     g_ptr[dev] = static_cast<uint32_t*>(p);
+    g_ctx_id[dev] = ctx;
   }
   *out = g_ptr[dev];
   return cudaSuccess;
@@ -92,10 +133,13 @@ extern "C" int pg_prune_reverse_noalloc(void* stream, const float* d_base, uint6
   uint32_t* w = nullptr;
   cudaError_t e = scratch_ptr(&w);
   if (e != cudaSuccess) return fail_na(PG_ECUDA, cudaGetErrorString(e));
-  int dev = 0, sms = 0;
+  int dev = 0, sdev = 0, sms = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+      (e = cudaStreamGetDevice(s, &sdev)) != cudaSuccess ||
       (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
     return fail_na(PG_ECUDA, cudaGetErrorString(e));
+  if (sdev != dev)
+    return fail_na(PG_EINVAL, "stream belongs to another device than the current one");
   unsigned long long* d_evals = reinterpret_cast<unsigned long long*>(w + kWCounters);
   uint32_t* d_status = w + kWCounters + 2;
   uint32_t* indeg = w + kWIndeg;
@@ -132,6 +176,5 @@ extern "C" int pg_prune_reverse_noalloc(void* stream, const float* d_base, uint6
   uint64_t ev = 0;
   std::memcpy(&ev, host, sizeof(ev));
   if (evals) *evals = ev;
-  if (host[2] != 0) return fail_na(PG_EINVAL, "input holds an id >= n that is not tomb");
-  return PG_OK;
+  return pg::status_error(host[2]);
 }

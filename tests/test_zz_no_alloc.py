@@ -37,11 +37,11 @@ def _outputs(n):
     return [torch.full(s, -1, dtype=torch.int32, device="cuda") for s in ((n, P), (n,), (n, R), (n,))]
 
 
-def _noalloc(pg, base, graph, outs, stream):
+def _noalloc(pg, base, graph, outs, stream, pruned=P):
     ev = ctypes.c_uint64(0)
     n, d = base.shape
     rc = pg.lib().pg_prune_reverse_noalloc(stream, base.data_ptr(), n, d, graph.data_ptr(),
-                                           graph.shape[1], P, R, 1, outs[0].data_ptr(),
+                                           graph.shape[1], pruned, R, 1, outs[0].data_ptr(),
                                            outs[1].data_ptr(), outs[2].data_ptr(),
                                            outs[3].data_ptr(), ctypes.byref(ev))
     return rc, int(ev.value)
@@ -101,3 +101,29 @@ def test_noalloc_rejects_sizes_beyond_its_limit(pg):
     rc, _ = _noalloc(pg, base, graph, outs, torch.cuda.current_stream().cuda_stream)
     assert rc == pg.PG_EINVAL
     assert b"32768" in pg.lib().pg_last_error()
+
+
+def test_noalloc_rejects_edge_count_beyond_its_limit(pg):
+    n, c, pruned = 32768, 64, 33  # n is allowed; n * pruned = 1081344 edges is not
+    base = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    graph = torch.full((n, c), -1, dtype=torch.int32, device="cuda")
+    outs = _outputs(n)
+    rc, _ = _noalloc(pg, base, graph, outs, torch.cuda.current_stream().cuda_stream, pruned=pruned)
+    assert rc == pg.PG_EINVAL
+    assert b"1048576" in pg.lib().pg_last_error()
+
+
+def test_noalloc_reports_out_of_range_id(pg, golden_dir):
+    """An input id >= n that is not tomb: the prune kernel drops it without reading its row and
+    flags it, and the call returns PG_EINVAL; the next call with good input succeeds."""
+    f = np.load(os.path.join(golden_dir, "ref_edge_1000x200.npz"))
+    bad = np.ascontiguousarray(f["search_in"]).copy()
+    bad[3, 5] = 1000 + 7
+    base = torch.from_numpy(np.ascontiguousarray(f["base"])).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    outs = _outputs(1000)
+    rc, _ = _noalloc(pg, base, torch.from_numpy(bad.view(np.int32)).cuda(), outs, stream)
+    assert rc == pg.PG_EINVAL
+    assert b"id >= n" in pg.lib().pg_last_error()
+    good = torch.from_numpy(np.ascontiguousarray(f["search_in"]).view(np.int32)).cuda()
+    assert _noalloc(pg, base, good, outs, stream)[0] == pg.PG_OK
