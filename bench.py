@@ -79,6 +79,9 @@ def parse():
     ap.add_argument("--max-points", type=int, default=500_000)
     ap.add_argument("--no-gt", action="store_true",
                     help="skip timing the exact ground-truth generation (pg_ground_truth)")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the 1M x 512 cosine (M=48, L=96) configuration timed beside the "
+                         "headline")
     ap.add_argument("--autotune", action="store_true",
                     help="run pg_autotune (launch shapes only; results unchanged) before timing")
     return ap.parse_args()
@@ -225,6 +228,87 @@ def search_roofline(st, args, peak_gbs, peak_kind, rounds):
                                "achieved": round(b0 / (st.ms_search[0] / 1e3) / 1e9, 1),
                                "traffic": dram[0] if dram else None,
                                "includes": "seed pre-pass + round-1 search"}
+    return out
+
+
+def screen_error_sample(base, graph, pairs: int = 1 << 20, seed: int = 7):
+    """Worst relative error |s16 - s64| / (|x||y|) over up to `pairs` graph edges (x, y): s16 is
+    the inner product of the FP16-rounded vectors accumulated in FP32 (what the screened prune
+    computes on tensor cores, in another order), s64 the FP64 inner product of the FP32 vectors."""
+    import torch
+    n = base.shape[0]
+    g = torch.Generator(device=base.device)
+    g.manual_seed(seed)
+    rows = torch.randint(0, n, (pairs,), generator=g, device=base.device)
+    cols = torch.randint(0, graph.shape[1], (pairs,), generator=g, device=base.device)
+    nb = graph[rows, cols].long()
+    ok = (nb >= 0) & (nb < n)
+    rows, nb = rows[ok], nb[ok]
+    worst = 0.0
+    for s in range(0, rows.numel(), 1 << 17):
+        x = base[rows[s:s + (1 << 17)]]
+        y = base[nb[s:s + (1 << 17)]]
+        s64 = (x.double() * y.double()).sum(1)
+        s16 = (x.half().float() * y.half().float()).sum(1)
+        scale = x.double().norm(dim=1) * y.double().norm(dim=1)
+        worst = max(worst, float(((s16.double() - s64).abs() / scale.clamp_min(1e-300)).max()))
+    return worst, int(rows.numel())
+
+
+def secondary_cosine(args, h, dev, stream):
+    """The precision configuration, measured beside the headline in the same run: 1M x 512, base
+    and queries L2-normalised (cosine), 128 centres, M = 48, L = 96, exact top-128 ground truth
+    (pg_ground_truth).  The FP16-screened build and the plain FP32 build are timed with CUDA events
+    on the handle's stream and their edges compared."""
+    import torch
+    import paragraph_gb300 as pg
+    from paragraph_gb300 import datagen
+    n, d, m, beam = 1_000_000, 512, 48, 96
+    base, _, queries = datagen.make_dataset_cuda(n, d, cosine=True, centers=128,
+                                                 seed=args.seed + 7, device=dev, with_gt=False)
+    gt = torch.empty((n, 128), dtype=torch.int32, device=dev)
+    h.ground_truth(base, queries, gt)
+    del queries
+    torch.cuda.empty_cache()
+    out = {"workload": f"ParaGraph build {n}x{d} cosine (128 centres), gt top-128 "
+                       f"(pg_ground_truth), M={m}, L={beam}"}
+    graphs = {}
+    for name, screen in (("fp16", pg.SCREEN_FP16), ("plain", pg.SCREEN_NONE)):
+        params = pg.default_params(m, beam, screen=screen)
+        graph = torch.empty((n, m), dtype=torch.int32, device=dev)
+        proj = torch.empty((n, 16), dtype=torch.int32, device=dev)
+        h.build_device(base, gt, graph, proj, params)  # warm-up
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        k = 2
+        e0.record(stream)
+        for _ in range(k):
+            st = h.build_device(base, gt, graph, proj, params)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        graphs[name] = (graph, proj)
+        out[name] = {"ms_per_build": round(ms, 2), "evals": int(st.evals_total),
+                     "evals_per_s": st.evals_total / (ms / 1e3),
+                     "stage_ms": {"proj": round(st.ms_proj, 2),
+                                  "search": [round(x, 2) for x in list(st.ms_search)[:2]],
+                                  "prune": [round(x, 2) for x in list(st.ms_prune)[:2]],
+                                  "merge": [round(x, 2) for x in list(st.ms_merge)[:2]]}}
+        if screen:
+            out[name]["rescored"] = list(st.rescored)[:2]
+            out[name]["occlusion_tests"] = list(st.evals_prune)[:2]
+    out["identical_edges"] = bool(torch.equal(graphs["fp16"][0], graphs["plain"][0]) and
+                                  torch.equal(graphs["fp16"][1], graphs["plain"][1]))
+    out["speedup_screened_vs_plain"] = round(out["plain"]["ms_per_build"] /
+                                             out["fp16"]["ms_per_build"], 3)
+    worst, npairs = screen_error_sample(base, graphs["plain"][0])
+    out["fp16_max_rel_error_vs_fp64"] = worst
+    out["error_sample"] = f"{npairs} random graph edges, |s16 - s64| / (|x||y|)"
+    dram = SEARCH_DRAM_BYTES.get((n, d, m, beam, True))
+    out["search_dram_bytes_per_launch"] = list(dram) if dram else None
+    del base, gt, graphs
+    torch.cuda.empty_cache()
     return out
 
 
@@ -443,6 +527,9 @@ def run_ours(args):
                                  "benchmark's own ground truth is a float32 top-k"}
         del gout, queries
         torch.cuda.empty_cache()
+    secondary = None
+    if not args.no_secondary and args.n == 1_000_000 and args.d == 200 and not args.cosine:
+        secondary = secondary_cosine(args, h, dev, stream)
     evals = stats[-1].evals_total
     assert all(s.evals_total == evals for s in stats), "evaluation count changed between builds"
     value = evals * args.steps * world / (ms_total / 1e3)
@@ -521,6 +608,7 @@ def run_ours(args):
                 "other_path": other_line,
                 "index": index_line,
                 "ground_truth": gt_line,
+                "secondary": secondary,
                 "gpu_launches": launches_per_build * args.steps,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary()}

@@ -201,12 +201,17 @@ int pg_build_index_host(pg_handle h, const pg_params* p, const float* base, uint
 /* ---- ground truth (the reference reads it from files made outside its build, README.md:25-31)
  * pg_ground_truth: for each of nq queries (nq x d, device) the k ids of the base rows (n x d)
  * with the largest inner product, best first -- exact: ranked by FP64 inner products, ties to the
- * lower id.  Candidates are screened on tensor cores (FP16 operands, FP32 accumulation) with a
- * rigorous error margin, and every candidate inside the margin is re-scored in FP64.  k <= 256;
- * rows past n are tomb.  PG_EUNSUPPORTED when a value exceeds the FP16 range (|x| > 65000) or the
- * margin holds more candidates than the selection can keep (1024 per query). */
+ * lower id.  Candidates are screened on the tensor cores (FP16 operands, FP32 accumulation, a
+ * tcgen05 GEMM whose epilogue selects: no score matrix is stored) with a rigorous error margin,
+ * and every candidate inside the margin is re-scored in FP64.  k <= 256, d <= 512; rows past n
+ * are tomb.  PG_EUNSUPPORTED when a value exceeds the FP16 range (|x| > 65000) or the margin
+ * holds more candidates than the selection can keep (1024 per query).
+ * pg_screen_scores: the screening product on its own, out (na x nb, FP32, device) =
+ * fp16(a) . fp16(b)^T with FP32 accumulation (a: na x d, b: nb x d, device, row-major). */
 int pg_ground_truth(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
                     const float* d_queries, uint64_t nq, uint32_t k, uint32_t* d_out);
+int pg_screen_scores(pg_handle h, const float* d_a, uint64_t na, const float* d_b, uint64_t nb,
+                     uint32_t d, float* d_out);
 
 /* ---- autotuning (no counterpart in the reference: its launch shapes, beam width and hash
  * capacity are compile-time constants, tests/test_t2iend.cu:671-727) --------------------------

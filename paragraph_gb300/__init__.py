@@ -125,6 +125,7 @@ SIGNATURES = {
                                            _U64, _U32, _U32, _U32, _U32, _VP, _VP,
                                            ctypes.POINTER(Stats)]),
     "pg_ground_truth": (ctypes.c_int, [_VP, _VP, _U64, _U32, _VP, _U64, _U32, _VP]),
+    "pg_screen_scores": (ctypes.c_int, [_VP, _VP, _U64, _VP, _U64, _U32, _VP]),
     "pg_set_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
     "pg_get_tuning": (ctypes.c_int, [_VP, ctypes.POINTER(Tuning)]),
     "pg_autotune": (ctypes.c_int, [_VP, ctypes.POINTER(Params), _VP, _U32, _VP, _VP, _VP, _U32,
@@ -365,6 +366,11 @@ class Handle:
         n, d = base.shape
         _check(lib().pg_ground_truth(self._h, _ptr(base), n, d, _ptr(queries), queries.shape[0],
                                      out.shape[1], _ptr(out)))
+
+    def screen_scores(self, a, b, out):
+        """pg_screen_scores: out (len(a) x len(b)) = fp16(a) . fp16(b)^T, FP32 accumulation."""
+        _check(lib().pg_screen_scores(self._h, _ptr(a), a.shape[0], _ptr(b), b.shape[0],
+                                      a.shape[1], _ptr(out)))
 
     def set_tuning(self, tuning: Tuning):
         _check(lib().pg_set_tuning(self._h, ctypes.byref(tuning)))

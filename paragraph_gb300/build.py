@@ -73,7 +73,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
     cudalib = os.path.join(os.path.dirname(os.path.dirname(cc)), "lib64")
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcublas", "-lcudart", "-Xlinker", "-rpath",
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-Xlinker", "-rpath",
            "-Xlinker", cudalib]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -9,7 +9,6 @@
 #include <string>
 #include <vector>
 
-#include <cublas_v2.h>
 
 #include "../../include/paragraph_gb300.h"
 #include "pg_kernels.h"
@@ -141,7 +140,6 @@ struct pg_handle_s {
   cudaGraphExec_t gexec = nullptr;  // captured build (PG_FLAG_CUDA_GRAPH) and what it was built for
   GraphKey gkey;
   pg_tuning tune{};  // launch shapes of later builds (zero = defaults)
-  cublasHandle_t blas = nullptr;  // pg_ground_truth's screening GEMM
   char* ws2 = nullptr;  // pg_build_index: graphs that outlive one stage (projection, link, rounds)
   size_t ws2_bytes = 0;
   cudaStream_t copy_stream = nullptr;  // pg_build_host: second host->device copy beside `stream`
@@ -770,7 +768,6 @@ int pg_destroy(pg_handle h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   cudaFree(h->ws);
   cudaFree(h->ws2);
-  if (h->blas) cublasDestroy(h->blas);
   cudaFree(h->inbuf);
   cudaFree(h->d_status);
   cudaFree(h->d_counters);
@@ -1499,40 +1496,57 @@ int pg_ground_truth(pg_handle h, const float* d_base, uint64_t n, uint32_t d,
   if (!h || !d_base || !d_queries || !d_out) return fail(PG_EINVAL, "NULL argument");
   if (n == 0 || n >= 0x7FFFFFFFull || nq == 0 || nq >= 0x7FFFFFFFull)
     return fail(PG_EINVAL, "n and nq must be in [1, 2^31-1)");
-  if (d == 0 || d % 4 != 0) return fail(PG_EUNSUPPORTED, "d=%u must be a positive multiple of 4", d);
+  if (d == 0 || d % 4 != 0 || d > pg::gt_max_dim())
+    return fail(PG_EUNSUPPORTED, "d=%u must be a positive multiple of 4, at most %u", d,
+                pg::gt_max_dim());
   if (k < 1 || k > pg::gt_max_k()) return fail(PG_EINVAL, "k=%u must be in [1, %u]", k, pg::gt_max_k());
   std::lock_guard<std::mutex> lk(h->mu);
   PG_CUDA(cudaSetDevice(h->device));
-  if (!h->blas) {
-    if (cublasCreate(&h->blas) != CUBLAS_STATUS_SUCCESS) {
-      h->blas = nullptr;
-      return fail(PG_ECUDA, "cublasCreate failed");
-    }
-    // FP32 accumulation everywhere, split-K reductions included
-    cublasSetMathMode(h->blas, static_cast<cublasMath_t>(
-                                   CUBLAS_DEFAULT_MATH |
-                                   CUBLAS_MATH_DISALLOW_REDUCED_PRECISION_REDUCTION));
-  }
-  int rc = ensure_ws(h, pg::gt_workspace_bytes(n, nq, d, 8));
+  const pg::GtPlan plan = pg::gt_plan(n, nq, d, h->num_sms, h->smem_optin);
+  int rc = ensure_ws(h, pg::gt_workspace_bytes(plan, n, nq));
   if (rc) return rc;
   PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, h->stream));
   // diagnostics in the counters' spare words: the first query's margin, max |x^|, max |x - x^|
   float* diag = reinterpret_cast<float*>(h->d_counters + 60);
-  const int r = pg::ground_truth(h->blas, d_base, n, d, d_queries, nq, k, d_out, h->ws,
+  const int r = pg::ground_truth(plan, d_base, n, d, d_queries, nq, k, d_out, h->ws,
                                  h->d_status, h->num_sms, h->stream, diag);
   if (r < 0) return fail(PG_ECUDA, "ground truth: %s", cudaGetErrorString(static_cast<cudaError_t>(-r)));
-  if (r > 0) return fail(PG_ECUDA, "ground truth: cuBLAS call failed (%d)", r);
+  if (r > 0) return fail(PG_ECUDA, "ground truth: cannot encode a TMA tensor map");
   PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, h->stream));
   PG_CUDA(cudaMemcpyAsync(h->h_counters + 60, diag, 12, cudaMemcpyDeviceToHost, h->stream));
   PG_CUDA(cudaStreamSynchronize(h->stream));
   const uint32_t st = *h->h_status;
   const float* dg = reinterpret_cast<const float*>(h->h_counters + 60);
   if (st & (1u << 4)) return fail(PG_EUNSUPPORTED, "ground truth: a value beyond the FP16 range");
-  if (st & ((1u << 5) | (1u << 6)))
+  if (st & (1u << 6))
     return fail(PG_EUNSUPPORTED,
                 "ground truth: more candidates within the screening margin than the selection "
                 "holds (status 0x%x; first query's margin %g, max |x| %g, max |x - fp16(x)| %g)",
                 st, dg[0], dg[1], dg[2]);
+  return status_to_error(st);
+}
+
+int pg_screen_scores(pg_handle h, const float* d_a, uint64_t na, const float* d_b, uint64_t nb,
+                     uint32_t d, float* d_out) {
+  if (!h || !d_a || !d_b || !d_out) return fail(PG_EINVAL, "NULL argument");
+  if (na == 0 || na >= 0x7FFFFFFFull || nb == 0 || nb >= 0x7FFFFFFFull)
+    return fail(PG_EINVAL, "na and nb must be in [1, 2^31-1)");
+  if (d == 0 || d % 4 != 0 || d > pg::gt_max_dim())
+    return fail(PG_EUNSUPPORTED, "d=%u must be a positive multiple of 4, at most %u", d,
+                pg::gt_max_dim());
+  std::lock_guard<std::mutex> lk(h->mu);
+  PG_CUDA(cudaSetDevice(h->device));
+  int rc = ensure_ws(h, pg::screen_scores_workspace(na, nb, d));
+  if (rc) return rc;
+  PG_CUDA(cudaMemsetAsync(h->d_status, 0, 4, h->stream));
+  const int r = pg::screen_scores(d_a, na, d_b, nb, d, d_out, h->ws, h->d_status, h->num_sms,
+                                  h->smem_optin, h->stream);
+  if (r < 0) return fail(PG_ECUDA, "screen scores: %s", cudaGetErrorString(static_cast<cudaError_t>(-r)));
+  if (r > 0) return fail(PG_ECUDA, "screen scores: cannot encode a TMA tensor map");
+  PG_CUDA(cudaMemcpyAsync(h->h_status, h->d_status, 4, cudaMemcpyDeviceToHost, h->stream));
+  PG_CUDA(cudaStreamSynchronize(h->stream));
+  const uint32_t st = *h->h_status;
+  if (st & (1u << 4)) return fail(PG_EUNSUPPORTED, "screen scores: a value beyond the FP16 range");
   return status_to_error(st);
 }
 

@@ -5,23 +5,29 @@
 // k base ids with the largest FP64 inner product q.x, ties to the lower id -- exact, whatever the
 // arithmetic used to find them.
 //
-//   1. FP16 copies of base and queries with per-row norms |x^| and |x - x^| (k_half_rows);
-//   2. screening scores s^ = q^.x^ by a cuBLAS FP16 GEMM with FP32 accumulation (tensor cores),
-//      a chunk of queries against all base rows at a time;
+//   1. FP16 copies of base and queries, rows zero-padded to a multiple of 64 elements, with
+//      per-row norms |x^| and |x - x^| (k_half_rows);
+//   2. screening scores s^ = q^.x^ on the tensor cores: k_gt_tc, a persistent tcgen05 GEMM
+//      (TMA-loaded 128-byte-swizzled tiles, FP32 accumulators in TMEM) whose epilogue consumes
+//      each 128 x 128 tile of scores in registers -- no score matrix is ever stored;
 //   3. a rigorous bound: |q.x - s^| <= E_q = (|q^| + |e_q|) max|e_x| + |e_q| max|x^|
 //      + g (|q^| max|x^|), with g covering the FP32 accumulation (d' * 2^-22, four times the
 //      IEEE unit roundoff, for the tensor core's accumulation);
-//   4. selection (k_gt_scan, eight warps per query row, one per row segment): a candidate
-//      buffer that keeps every score >= (running k-th largest) - 2 E_q, compacted by a warp
-//      radix select when full; then (k_gt_final) the row's k-th largest screened score t_k
-//      over the segments' lists (radix select again), and the candidates with
-//      s^ >= t_k - 2 E_q, a superset of the true top-k;
-//   5. exact FP64 inner products of the candidates and a sort by (score desc, id asc).
-// On the benchmark's data a query keeps about 1.1 k candidates.
-#include <cublas_v2.h>
+//   4. pass 1 (k_gt_tc<kMax>): the maximum screened score of every group of gs consecutive base
+//      rows per query; the k-th largest group maximum theta_q is the score of k distinct base
+//      rows, so theta_q <= t_k, the k-th largest screened score of the row (k_gt_theta);
+//   5. pass 2 (k_gt_tc<kFilter>): every base row with s^ >= theta_q - 2 E_q is a candidate --
+//      a superset of {s^ >= t_k - 2 E_q}, which holds the true top k (a true top-k member has
+//      s^ >= s_k - E_q and s_k >= t_k - E_q);
+//   6. k_gt_final: the candidates with s^ >= t_k - 2 E_q, exact FP64 inner products, sorted by
+//      (score desc, id asc).
+// With groups small enough that the top k fall in distinct groups (G = n / gs >= 8192 where n
+// allows), theta_q sits just below t_k and a query keeps about 1.1 k candidates.
+#include <cuda.h>
 #include <cuda_fp16.h>
 
 #include <cmath>
+#include <mutex>
 
 #include "pg_device.cuh"
 #include "pg_kernels.h"
@@ -30,14 +36,12 @@ namespace pg {
 
 namespace {
 
-constexpr uint32_t kGtCap = 1024;  // candidate buffer per warp
+constexpr uint32_t kGtCap = 1024;          // candidates per query
 constexpr uint32_t kGtErrRange = 1u << 4;  // a value beyond the FP16 range
-constexpr uint32_t kGtErrScan = 1u << 5;   // a row segment kept more candidates than kGtCap
-constexpr uint32_t kGtErrFinal = 1u << 6;  // a row kept more candidates than kGtCap
-constexpr int kScanWarps = 4;
+constexpr uint32_t kGtErrFinal = 1u << 6;  // a query kept more candidates than kGtCap
 constexpr int kFinalWarps = 2;
 
-__device__ __forceinline__ float key_value(uint64_t key) {  // inverse of the key below
+__device__ __forceinline__ float key_value(uint64_t key) {  // inverse of desc_key's value part
   const uint32_t o = ~static_cast<uint32_t>(key >> 32);
   const uint32_t u = (o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o;
   return __uint_as_float(u);
@@ -54,7 +58,9 @@ __device__ __forceinline__ uint64_t desc_key64(double v) {  // descending double
   return ~o;
 }
 
-__global__ void k_half_rows(const float* __restrict__ x, uint64_t rows, uint32_t d,
+// FP16 copy of rows x d FP32 values with row stride dp >= d (zeros in the padding), and per row
+// upper bounds of |x^| and |x - x^| (FP64 sums rounded up).
+__global__ void k_half_rows(const float* __restrict__ x, uint64_t rows, uint32_t d, uint32_t dp,
                             __half* __restrict__ h, float* __restrict__ nrm,
                             float* __restrict__ enrm, uint32_t* __restrict__ status) {
   const uint32_t lane = lane_id();
@@ -63,11 +69,15 @@ __global__ void k_half_rows(const float* __restrict__ x, uint64_t rows, uint32_t
        r < rows; r += nw) {
     double a = 0.0, e = 0.0;
     bool big = false;
-    for (uint32_t i = lane; i < d; i += 32) {
+    for (uint32_t i = lane; i < dp; i += 32) {
+      if (i >= d) {
+        h[r * dp + i] = __float2half_rn(0.0f);
+        continue;
+      }
       const float v = x[r * d + i];
       big |= !(fabsf(v) <= 65000.0f);  // beyond FP16 range (or NaN)
       const __half hv = __float2half_rn(v);
-      h[r * d + i] = hv;
+      h[r * dp + i] = hv;
       const double fv = static_cast<double>(__half2float(hv));
       a = fma(fv, fv, a);
       const double ev = static_cast<double>(v) - fv;
@@ -105,33 +115,21 @@ __global__ void k_max2(const float* __restrict__ a, const float* __restrict__ b,
 }
 
 // Per query of the chunk: 2 E_q plus a relative slack for the FP32 arithmetic of the threshold.
+// The tensor core accumulates over dp (d plus zero padding) products.
 __global__ void k_gt_band(const float* __restrict__ qn, const float* __restrict__ qe,
-                          const uint32_t* __restrict__ xmax, uint32_t rows, uint32_t d,
+                          const uint32_t* __restrict__ xmax, uint32_t rows, uint32_t dp,
                           float* __restrict__ band) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= rows) return;
   const double xn = __uint_as_float(xmax[0]), xe = __uint_as_float(xmax[1]);
-  const double dd = d + 16.0, u = 1.0 / 4194304.0;  // 2^-22
+  const double dd = dp + 16.0, u = 1.0 / 4194304.0;  // 2^-22
   const double g = dd * u / (1.0 - dd * u);
   const double q = qn[r], e = qe[r];
   const double E = (q + e) * xe + e * xn + g * q * xn;
   band[r] = __double2float_ru(2.0 * E * (1.0 + 1e-6) + 1e-30);
 }
 
-struct GtArgs {
-  const float* scores;  // rows x n
-  uint64_t n;
-  uint32_t rows, k, segs;
-  const float* band;     // rows
-  uint64_t* seg_keys;    // rows x segs x kGtCap
-  uint32_t* seg_cnt;     // rows x segs
-  float* seg_theta;      // rows x segs (k-th largest of the segment, or -inf)
-  const float* base;     // n x d (FP32)
-  const float* queries;  // rows x d (FP32, this chunk)
-  uint32_t d;
-  uint32_t* out;  // rows x k
-  uint32_t* status;
-};
+// ---------------------------------------------------------------- selection helpers
 
 // Sorts buf[0 .. cnt) (desc value, asc id); returns the k-th largest value (or -inf when
 // cnt < k) and keeps in buf the prefix with value >= that - band; *cnt updated.
@@ -169,17 +167,24 @@ __device__ float compact_sorted(uint64_t* buf, uint32_t& cnt, uint32_t k, float 
   return theta;
 }
 
-// The k-th smallest of the keys' upper 32 bits (the k-th largest value) among buf[0 .. cnt),
-// by a four-pass 8-bit radix select with a 256-bin histogram in shared memory; loops, not an
-// unrolled network, so the scan kernel stays small.  Requires cnt >= k.
-__device__ uint32_t radix_kth(const uint64_t* buf, uint32_t cnt, uint32_t k, uint32_t* hist) {
+__device__ float compact_any(uint64_t* buf, uint32_t& cnt, uint32_t k, float band) {
+  if (cnt <= 128) return compact_sorted<4>(buf, cnt, k, band);
+  if (cnt <= 256) return compact_sorted<8>(buf, cnt, k, band);
+  if (cnt <= 512) return compact_sorted<16>(buf, cnt, k, band);
+  return compact_sorted<32>(buf, cnt, k, band);
+}
+
+// The k-th smallest of key(0 .. cnt-1) (32-bit keys), by a four-pass 8-bit radix select with a
+// 256-bin histogram in shared memory.  Requires cnt >= k.  One warp.
+template <class Key>
+__device__ uint32_t radix_kth(Key key, uint32_t cnt, uint32_t k, uint32_t* hist) {
   const uint32_t lane = lane_id();
   uint32_t prefix = 0, mask = 0, rem = k;
   for (int shift = 24; shift >= 0; shift -= 8) {
     for (uint32_t b = lane; b < 256; b += 32) hist[b] = 0;
     __syncwarp();
     for (uint32_t i = lane; i < cnt; i += 32) {
-      const uint32_t vk = static_cast<uint32_t>(buf[i] >> 32);
+      const uint32_t vk = key(i);
       if ((vk & mask) == prefix) atomicAdd(hist + ((vk >> shift) & 255u), 1u);
     }
     __syncwarp();
@@ -221,172 +226,17 @@ __device__ uint32_t radix_kth(const uint64_t* buf, uint32_t cnt, uint32_t k, uin
   return prefix;
 }
 
-// radix_kth over the union of a row's segment lists in global memory (seg_keys / seg_cnt).
-__device__ uint32_t radix_kth_segs(const uint64_t* keys, const uint32_t* cnts, uint32_t segs,
-                                   uint32_t k, uint32_t* hist) {
-  const uint32_t lane = lane_id();
-  uint32_t prefix = 0, mask = 0, rem = k;
-  for (int shift = 24; shift >= 0; shift -= 8) {
-    for (uint32_t b = lane; b < 256; b += 32) hist[b] = 0;
-    __syncwarp();
-    for (uint32_t sg = 0; sg < segs; sg++) {
-      const uint64_t* src = keys + static_cast<uint64_t>(sg) * kGtCap;
-      const uint32_t c = cnts[sg];
-      for (uint32_t i = lane; i < c; i += 32) {
-        const uint32_t vk = static_cast<uint32_t>(src[i] >> 32);
-        if ((vk & mask) == prefix) atomicAdd(hist + ((vk >> shift) & 255u), 1u);
-      }
-    }
-    __syncwarp();
-    uint32_t local[8], sum = 0;
-#pragma unroll
-    for (int t = 0; t < 8; t++) {
-      local[t] = hist[lane * 8 + t];
-      sum += local[t];
-    }
-    uint32_t incl = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(kFull, incl, o);
-      if (lane >= static_cast<uint32_t>(o)) incl += y;
-    }
-    const uint32_t excl = incl - sum;
-    const unsigned owner = __ballot_sync(kFull, excl < rem && rem <= incl);
-    const uint32_t src_lane = static_cast<uint32_t>(__ffs(static_cast<int>(owner)) - 1);
-    uint32_t bin = 0, before = 0;
-    if (lane == src_lane) {
-      uint32_t c = excl;
-#pragma unroll
-      for (int t = 0; t < 8; t++) {
-        if (c + local[t] >= rem) {
-          bin = lane * 8 + t;
-          before = c;
-          break;
-        }
-        c += local[t];
-      }
-    }
-    bin = __shfl_sync(kFull, bin, src_lane);
-    before = __shfl_sync(kFull, before, src_lane);
-    prefix |= bin << shift;
-    mask |= 255u << shift;
-    rem -= before;
-    __syncwarp();
-  }
-  return prefix;
-}
-
-// Keeps (in place, order not kept) the entries of buf[0 .. cnt) whose value is >= the k-th
-// largest value minus band; returns that k-th largest value (-inf when cnt < k).
-__device__ float compact_select(uint64_t* buf, uint32_t& cnt, uint32_t k, float band,
-                                uint32_t* hist) {
-  const uint32_t lane = lane_id();
-  if (cnt < k) return -INFINITY;
-  const uint32_t kv = radix_kth(buf, cnt, k, hist);
-  const float theta = key_value(static_cast<uint64_t>(kv) << 32);
-  const float lo = theta - band;
-  uint32_t out = 0;
-  for (uint32_t i0 = 0; i0 < cnt; i0 += 32) {
-    const uint32_t i = i0 + lane;
-    const uint64_t key = i < cnt ? buf[i] : ~0ull;
-    const bool ok = i < cnt && key_value(key) >= lo;
-    const unsigned m = __ballot_sync(kFull, ok);
-    __syncwarp();
-    if (ok) buf[out + __popc(m & ((1u << lane) - 1u))] = key;
-    out += __popc(m);
-    __syncwarp();
-  }
-  cnt = out;
-  return theta;
-}
-
-__device__ float compact_any(uint64_t* buf, uint32_t& cnt, uint32_t k, float band) {
-  if (cnt <= 128) return compact_sorted<4>(buf, cnt, k, band);
-  if (cnt <= 256) return compact_sorted<8>(buf, cnt, k, band);
-  if (cnt <= 512) return compact_sorted<16>(buf, cnt, k, band);
-  return compact_sorted<32>(buf, cnt, k, band);
-}
-
-// One warp per (query row, row segment): every screened score that may be in the top k.
-__global__ void __launch_bounds__(kScanWarps * 32) k_gt_scan(GtArgs a) {
-  __shared__ uint64_t buf_all[kScanWarps][kGtCap];
-  __shared__ uint32_t hist_all[kScanWarps][256];
-  uint64_t* buf = buf_all[threadIdx.x >> 5];
-  uint32_t* hist = hist_all[threadIdx.x >> 5];
-  const uint32_t lane = lane_id();
-  const uint64_t nw = static_cast<uint64_t>(gridDim.x) * kScanWarps;
-  // segments start on 512-value boundaries: one pass of the loop below reads 512 values per
-  // warp, 16 per lane as four 16-byte loads (when rows are 16-byte aligned, n % 4 == 0)
-  const uint64_t seglen = ((a.n + a.segs - 1) / a.segs + 511) & ~511ull;
-  const bool vec = (a.n & 3u) == 0;
-  for (uint64_t w = blockIdx.x * static_cast<uint64_t>(kScanWarps) + (threadIdx.x >> 5);
-       w < static_cast<uint64_t>(a.rows) * a.segs; w += nw) {
-    const uint64_t row = w / a.segs, seg = w % a.segs;
-    const uint64_t x0 = min(a.n, seg * seglen), x1 = min(a.n, x0 + seglen);
-    const float band = a.band[row];
-    const float* srow = a.scores + row * a.n;
-    uint32_t cnt = 0;
-    float theta = -INFINITY;
-    bool over = false;
-    for (uint64_t xb = x0; xb < x1 && !over; xb += 512) {
-      float v[16];
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const uint64_t p = xb + 128u * j + 4u * lane;
-        if (vec && p + 3 < x1) {
-          const float4 f = __ldg(reinterpret_cast<const float4*>(srow + p));
-          v[4 * j] = f.x;
-          v[4 * j + 1] = f.y;
-          v[4 * j + 2] = f.z;
-          v[4 * j + 3] = f.w;
-        } else {
-#pragma unroll
-          for (int t = 0; t < 4; t++) v[4 * j + t] = p + t < x1 ? srow[p + t] : -INFINITY;
-        }
-      }
-      float mx = v[0];
-#pragma unroll
-      for (int j = 1; j < 16; j++) mx = fmaxf(mx, v[j]);
-      if (!__any_sync(kFull, mx >= theta - band)) continue;  // the common case once warm
-#pragma unroll
-      for (int j = 0; j < 16; j++) {
-        const uint64_t xi = xb + 128u * (j >> 2) + 4u * lane + (j & 3);
-        bool pass = xi < x1 && v[j] >= theta - band;
-        unsigned m = __ballot_sync(kFull, pass);
-        if (!m) continue;
-        if (cnt + __popc(m) > kGtCap) {
-          theta = compact_select(buf, cnt, a.k, band, hist);
-          pass = xi < x1 && v[j] >= theta - band;
-          m = __ballot_sync(kFull, pass);
-          if (cnt + __popc(m) > kGtCap) {
-            over = true;
-            break;
-          }
-        }
-        if (pass)
-          buf[cnt + __popc(m & ((1u << lane) - 1u))] = desc_key(v[j], static_cast<uint32_t>(xi));
-        cnt += __popc(m);
-        __syncwarp();
-      }
-    }
-    if (over) {
-      if (lane == 0) {
-        raise_error(a.status, kGtErrScan);
-        a.seg_cnt[w] = 0;
-        a.seg_theta[w] = -INFINITY;
-      }
-      continue;
-    }
-    theta = compact_select(buf, cnt, a.k, band, hist);
-    uint64_t* dst = a.seg_keys + w * kGtCap;
-    for (uint32_t i = lane; i < cnt; i += 32) dst[i] = buf[i];
-    if (lane == 0) {
-      a.seg_cnt[w] = cnt;
-      a.seg_theta[w] = theta;
-    }
-    __syncwarp();
-  }
-}
+struct GtArgs {
+  const float* base;     // n x d (FP32)
+  const float* queries;  // rows x d (FP32, this chunk)
+  uint32_t d, k;
+  uint32_t rows;
+  const uint64_t* cand;      // rows x kGtCap keys (desc_key)
+  const uint32_t* cand_cnt;  // rows
+  const float* band;         // rows
+  uint32_t* out;             // rows x k
+  uint32_t* status;
+};
 
 // Exact FP64 scores of the candidates c = buf[0 .. cnt), sorted by (score desc, id asc); the
 // first k ids go to out (tomb past cnt).
@@ -430,7 +280,7 @@ __device__ void rescore_write(const GtArgs& a, uint64_t row, const uint64_t* buf
   }
   __syncwarp();
   if (__any_sync(kFull, tie)) {
-    uint64_t* ks = reinterpret_cast<uint64_t*>(const_cast<uint64_t*>(buf));  // reuse as keys
+    uint64_t* ks = const_cast<uint64_t*>(buf);  // reuse as keys
 #pragma unroll
     for (int s = 0; s < E; s++) {
       const uint32_t i = static_cast<uint32_t>(s) * 32u + lane;
@@ -455,56 +305,22 @@ __device__ void rescore_write(const GtArgs& a, uint64_t row, const uint64_t* buf
   __syncwarp();
 }
 
+// One warp per query: its candidates (those with s^ >= theta - 2 E_q), then the ones with
+// s^ >= t_k - 2 E_q, re-scored in FP64 and sorted.
 __global__ void __launch_bounds__(kFinalWarps * 32) k_gt_final(GtArgs a) {
   __shared__ uint64_t buf_all[kFinalWarps][kGtCap];
   __shared__ uint32_t ids_all[kFinalWarps][kGtCap];
-  __shared__ uint32_t hist_all[kFinalWarps][256];
-  uint32_t* hist = hist_all[threadIdx.x >> 5];
   uint64_t* buf = buf_all[threadIdx.x >> 5];
   uint32_t* ids_s = ids_all[threadIdx.x >> 5];
   const uint32_t lane = lane_id();
   const uint64_t nw = static_cast<uint64_t>(gridDim.x) * kFinalWarps;
   for (uint64_t row = blockIdx.x * static_cast<uint64_t>(kFinalWarps) + (threadIdx.x >> 5);
        row < a.rows; row += nw) {
-    const float band = a.band[row];
-    // pass 1: the row's k-th largest screened score t_k over the union of the segment lists
-    // (each holds its own segment's top k)
-    uint32_t total = 0;
-    for (uint32_t s = 0; s < a.segs; s++) total += a.seg_cnt[row * a.segs + s];
-    const float tk = total >= a.k
-                         ? key_value(static_cast<uint64_t>(radix_kth_segs(
-                                         a.seg_keys + row * a.segs * kGtCap,
-                                         a.seg_cnt + row * a.segs, a.segs, a.k, hist))
-                                     << 32)
-                         : -INFINITY;
-    // pass 2: every screened score >= t_k - band, from the whole segment lists
-    const float lo = tk - band;
-    uint32_t cnt = 0;
-    bool over = false;
-    for (uint32_t s = 0; s < a.segs && !over; s++) {
-      const uint64_t w = row * a.segs + s;
-      const uint32_t c = a.seg_cnt[w];
-      const uint64_t* src = a.seg_keys + w * kGtCap;
-      for (uint32_t i0 = 0; i0 < c; i0 += 32) {
-        const uint32_t i = i0 + lane;
-        const uint64_t key = i < c ? src[i] : ~0ull;
-        const bool ok = i < c && key_value(key) >= lo;
-        const unsigned m = __ballot_sync(kFull, ok);
-        if (cnt + __popc(m) > kGtCap) {
-          over = true;
-          break;
-        }
-        if (ok) buf[cnt + __popc(m & ((1u << lane) - 1u))] = key;
-        cnt += __popc(m);
-      }
-    }
+    uint32_t cnt = min(a.cand_cnt[row], kGtCap);
+    const uint64_t* src = a.cand + row * kGtCap;
+    for (uint32_t i = lane; i < cnt; i += 32) buf[i] = src[i];
     __syncwarp();
-    if (over) {
-      if (lane == 0) raise_error(a.status, kGtErrFinal);
-      for (uint32_t i = lane; i < a.k; i += 32) a.out[row * a.k + i] = kTomb;
-      continue;
-    }
-    compact_any(buf, cnt, a.k, band);  // candidates >= t_k - band, sorted
+    compact_any(buf, cnt, a.k, a.band[row]);  // candidates >= t_k - band, sorted
     if (cnt <= 128)
       rescore_write<4>(a, row, buf, cnt, ids_s);
     else if (cnt <= 256)
@@ -516,6 +332,441 @@ __global__ void __launch_bounds__(kFinalWarps * 32) k_gt_final(GtArgs a) {
   }
 }
 
+// One warp per query: lo = theta - 2 E_q, theta the k-th largest of the row's group maxima
+// (-inf when there are fewer than k groups: every base row is then a candidate).
+__global__ void __launch_bounds__(256) k_gt_theta(const float* __restrict__ maxima,
+                                                  uint32_t rows, uint32_t groups, uint32_t k,
+                                                  const float* __restrict__ band,
+                                                  float* __restrict__ lo) {
+  __shared__ uint32_t hist_all[8][256];
+  uint32_t* hist = hist_all[threadIdx.x >> 5];
+  const uint64_t nw = static_cast<uint64_t>(gridDim.x) * 8;
+  for (uint64_t row = blockIdx.x * 8ull + (threadIdx.x >> 5); row < rows; row += nw) {
+    if (groups < k) {
+      if (lane_id() == 0) lo[row] = -INFINITY;
+      continue;
+    }
+    const float* m = maxima + row * groups;
+    const uint32_t kv =
+        radix_kth([m](uint32_t i) { return ~order_key(m[i]); }, groups, k, hist);
+    const float theta = key_value(static_cast<uint64_t>(kv) << 32);
+    if (lane_id() == 0) lo[row] = theta - band[row];
+  }
+}
+
+// ---------------------------------------------------------------- tcgen05 screening GEMM
+//
+// D (128 queries x 128 base rows, FP32 in TMEM) = A (queries, FP16, K-major) . B (base rows,
+// FP16, K-major)^T, K = dp in boxes of 64 elements (one 128-byte swizzled row per box row).
+// One CTA per SM, persistent over query tiles of 128 * mt rows (mt = 1 or 2 M tiles sharing each
+// B tile); for each query tile it sweeps every base tile in order:
+//   warp 0      TMA producer: A tiles once per query tile, B boxes through a kStages ring;
+//   warp 1      TMEM owner and MMA issuer (one thread): 4 MMAs (K = 16) per box per M tile,
+//               into one of two accumulator buffers per M tile;
+//   warps 2..5  epilogue: TMEM -> registers (warp w reads TMEM lanes 32 (w % 4) ..), one thread
+//               per query row, the mode's work on 128 scores per M tile, then the buffer is
+//               released.
+// Every wait is bounded (1 s); a wait that gives up raises kErrWait, the CTA's roles stop, the
+// issued MMAs are drained and the TMEM is freed before the CTA exits.
+namespace tc {
+
+constexpr uint32_t kRows = 128;  // rows of an A tile (queries) and of a B tile (base rows)
+constexpr uint32_t kChunk = 64;  // K elements per TMA box
+constexpr uint32_t kBox = kRows * kChunk * 2;  // 16 KB
+constexpr uint32_t kStages = 5;
+constexpr uint32_t kThreads = 192;
+constexpr uint32_t kMaxKc = 8;  // dp <= 512
+// kind::f16 instruction descriptor: FP32 accumulator (bits 4-5 = 1), A and B FP16 (0), both
+// K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | ((kRows >> 3) << 17) | ((kRows >> 4) << 24);
+
+enum Mode : int { kMax = 0, kFilter = 1, kDump = 2 };
+
+struct Args {
+  uint32_t q0;      // first row of this chunk in the query tensor map
+  uint32_t nq;      // query rows of this chunk
+  uint32_t n;       // base rows
+  uint32_t kc;      // K boxes per row: dp / 64
+  uint32_t mt;      // M tiles per query tile (1 or 2)
+  uint32_t gs;      // kMax: group size (power of two)
+  uint32_t groups;  // kMax: ceil(n / gs)
+  float* maxima;    // kMax: nq x groups
+  const float* lo;  // kFilter: nq thresholds
+  uint64_t* cand;   // kFilter: nq x kGtCap keys
+  uint32_t* cand_cnt;  // kFilter: nq
+  float* dump;      // kDump: nq x n scores
+  uint32_t* status;
+};
+
+__device__ __forceinline__ uint32_t saddr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint64_t now_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void bar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(b)) : "memory");
+}
+__device__ __forceinline__ bool bar_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(saddr(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for the phase of parity `parity` of *b; false after one second or when another role
+// has given up (*stop set).
+__device__ __forceinline__ bool bar_wait(uint64_t* b, uint32_t parity,
+                                         const volatile uint32_t* stop) {
+  if (bar_try(b, parity)) return true;
+  const uint64_t t0 = now_ns();
+  for (uint32_t i = 1;; i++) {
+    if (bar_try(b, parity)) return true;
+    if ((i & 31u) == 0) {
+      if (stop && *stop) return false;
+      if (now_ns() - t0 > 1000000000ull) return false;
+    }
+  }
+}
+__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, uint32_t x,
+                                         uint32_t y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(saddr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(saddr(bar))
+      : "memory");
+}
+// Shared-memory descriptor of a K-major tile written by TMA with 128-byte swizzling: rows of
+// 128 bytes in 8-row atoms of 1024 bytes (stride byte offset), one atom along K (leading byte
+// offset unused), descriptor version 1 (bits 46-47), swizzle mode 2 (bits 61-63).  The start
+// address steps 32 bytes per K = 16 slice inside the atom.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) | (static_cast<uint64_t>(1024 >> 4) << 32) |
+         (1ull << 46) | (2ull << 61);
+}
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          saddr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+size_t smem_bytes(uint32_t mt, uint32_t kc) {
+  return 1024 + static_cast<size_t>(mt) * kc * kBox + kStages * kBox + 256;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_gt_tc(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+            const Args a) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  uint8_t* sm = smem_raw + ((1024u - (saddr(smem_raw) & 1023u)) & 1023u);
+  uint8_t* sA = sm;  // mt x kc boxes
+  uint8_t* sB = sA + static_cast<size_t>(a.mt) * a.kc * kBox;  // kStages boxes
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + kStages * kBox);
+  uint64_t* empty = full + kStages;
+  uint64_t* a_full = empty + kStages;
+  uint64_t* a_empty = a_full + 1;
+  uint64_t* t_full = a_empty + 1;   // [2]
+  uint64_t* t_empty = t_full + 2;   // [2]
+  uint64_t* drained = t_empty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drained + 1);
+  volatile uint32_t* stop = tmem_slot + 1;
+
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint32_t rows_per_tile = kRows * a.mt;
+  const uint32_t q_tiles = (a.nq + rows_per_tile - 1) / rows_per_tile;
+  const uint32_t n_tiles = (a.n + kRows - 1) / kRows;
+  const uint32_t ncols = 256u * a.mt;  // two accumulator buffers of 128 columns per M tile
+
+  if (threadIdx.x == 0) {
+    for (uint32_t s = 0; s < kStages; s++) {
+      bar_init(full + s, 1);
+      bar_init(empty + s, 1);
+    }
+    bar_init(a_full, 1);
+    bar_init(a_empty, 1);
+    for (int b = 0; b < 2; b++) {
+      bar_init(t_full + b, 1);
+      bar_init(t_empty + b, kRows);
+    }
+    bar_init(drained, 1);
+    *stop = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     saddr(tmem_slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---- TMA producer
+    if (lane == 0) {
+      bool ok = true;
+      uint32_t it = 0, sti = 0;
+      for (uint32_t st = blockIdx.x; ok && st < q_tiles; st += gridDim.x, sti++) {
+        if (!bar_wait(a_empty, (sti & 1u) ^ 1u, stop)) {
+          ok = false;
+          break;
+        }
+        bar_expect_tx(a_full, a.mt * a.kc * kBox);
+        for (uint32_t m = 0; m < a.mt; m++)
+          for (uint32_t c = 0; c < a.kc; c++)
+            tma_load(sA + (m * a.kc + c) * kBox, &ta, c * kChunk,
+                     a.q0 + st * rows_per_tile + m * kRows, a_full);
+        for (uint32_t bt = 0; ok && bt < n_tiles; bt++)
+          for (uint32_t c = 0; c < a.kc; c++, it++) {
+            const uint32_t s = it % kStages, ph = (it / kStages) & 1u;
+            if (!bar_wait(empty + s, ph ^ 1u, stop)) {
+              ok = false;
+              break;
+            }
+            bar_expect_tx(full + s, kBox);
+            tma_load(sB + s * kBox, &tb, c * kChunk, bt * kRows, full + s);
+          }
+      }
+      if (!ok) {
+        raise_error(a.status, kErrWait);
+        *stop = 1;
+      }
+      // the loads still in flight land before the CTA exits: each stage's last issued load
+      for (uint32_t j = 0; j < kStages && j < it; j++) {
+        const uint32_t i = it - 1 - j;
+        bar_wait(full + (i % kStages), (i / kStages) & 1u, nullptr);
+      }
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer
+    if (lane == 0) {
+      bool ok = true;
+      uint32_t it = 0, t = 0, sti = 0;
+      const uint32_t a0 = saddr(sA), b0 = saddr(sB);
+      for (uint32_t st = blockIdx.x; ok && st < q_tiles; st += gridDim.x, sti++) {
+        if (!bar_wait(a_full, sti & 1u, stop)) {
+          ok = false;
+          break;
+        }
+        fence_after();
+        for (uint32_t bt = 0; ok && bt < n_tiles; bt++, t++) {
+          const uint32_t buf = t & 1u, use = t >> 1;
+          if (!bar_wait(t_empty + buf, (use & 1u) ^ 1u, stop)) {
+            ok = false;
+            break;
+          }
+          fence_after();
+          for (uint32_t c = 0; c < a.kc; c++, it++) {
+            const uint32_t s = it % kStages, ph = (it / kStages) & 1u;
+            if (!bar_wait(full + s, ph, stop)) {
+              ok = false;
+              break;
+            }
+            fence_after();
+            for (uint32_t m = 0; m < a.mt; m++)
+#pragma unroll
+              for (uint32_t k = 0; k < 4; k++)
+                mma(tmem + (m * 2 + buf) * kRows, sw128_desc(a0 + (m * a.kc + c) * kBox + k * 32),
+                    sw128_desc(b0 + s * kBox + k * 32), (c | k) != 0);
+            commit(empty + s);  // the stage is free once these MMAs have read it
+          }
+          if (ok) commit(t_full + buf);
+        }
+        if (ok) commit(a_empty);
+      }
+      if (!ok) {
+        raise_error(a.status, kErrWait);
+        *stop = 1;
+      }
+      commit(drained);  // arrives when every MMA issued above has completed
+      bar_wait(drained, 0, nullptr);
+    }
+  } else {
+    // ---- epilogue: one thread per query row of each M tile
+    const uint32_t quarter = warp & 3u;
+    const uint32_t row = quarter * 32u + lane;
+    const uint32_t lane_base = (quarter * 32u) << 16;
+    bool ok = true;
+    uint32_t t = 0;
+    for (uint32_t st = blockIdx.x; ok && st < q_tiles; st += gridDim.x) {
+      uint32_t qrow[2], cnt[2] = {0, 0};
+      bool valid[2];
+      float lo[2], gmax[2] = {-INFINITY, -INFINITY};
+      for (uint32_t m = 0; m < 2; m++) {
+        qrow[m] = st * rows_per_tile + m * kRows + row;
+        valid[m] = m < a.mt && qrow[m] < a.nq;
+        lo[m] = (MODE == kFilter && valid[m]) ? a.lo[qrow[m]] : INFINITY;
+      }
+      for (uint32_t bt = 0; bt < n_tiles; bt++, t++) {
+        const uint32_t buf = t & 1u, use = t >> 1;
+        ok = __all_sync(kFull, bar_wait(t_full + buf, use & 1u, stop));
+        if (!ok) break;
+        fence_after();
+        for (uint32_t m = 0; m < a.mt; m++) {
+#pragma unroll 1
+          for (uint32_t ch = 0; ch < 4; ch++) {
+            uint32_t v[32];
+            tmem_ld32(tmem + lane_base + (m * 2 + buf) * kRows + ch * 32, v);
+            if (!valid[m]) continue;
+            const uint32_t col0 = bt * kRows + ch * 32;
+            if (MODE == kMax) {
+#pragma unroll
+              for (uint32_t j = 0; j < 32; j++) {
+                const uint32_t c = col0 + j;
+                if (c < a.n) {
+                  gmax[m] = fmaxf(gmax[m], __uint_as_float(v[j]));
+                  if (((c + 1) & (a.gs - 1)) == 0 || c + 1 == a.n) {
+                    a.maxima[static_cast<uint64_t>(qrow[m]) * a.groups + c / a.gs] = gmax[m];
+                    gmax[m] = -INFINITY;
+                  }
+                }
+              }
+            } else if (MODE == kFilter) {
+#pragma unroll
+              for (uint32_t j = 0; j < 32; j++) {
+                const uint32_t c = col0 + j;
+                const float x = __uint_as_float(v[j]);
+                if (c < a.n && x >= lo[m]) {
+                  if (cnt[m] < kGtCap)
+                    a.cand[static_cast<uint64_t>(qrow[m]) * kGtCap + cnt[m]] = desc_key(x, c);
+                  cnt[m]++;
+                }
+              }
+            } else {
+              float* o = a.dump + static_cast<uint64_t>(qrow[m]) * a.n;
+#pragma unroll
+              for (uint32_t j = 0; j < 32; j++)
+                if (col0 + j < a.n) o[col0 + j] = __uint_as_float(v[j]);
+            }
+          }
+        }
+        fence_before();
+        bar_arrive(t_empty + buf);
+      }
+      if (MODE == kFilter && ok)
+        for (uint32_t m = 0; m < a.mt; m++)
+          if (valid[m]) {
+            a.cand_cnt[qrow[m]] = min(cnt[m], kGtCap);
+            if (cnt[m] > kGtCap) raise_error(a.status, kGtErrFinal);
+          }
+    }
+    if (!ok && lane == 0) {
+      raise_error(a.status, kErrWait);
+      *stop = 1;
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(ncols)
+                 : "memory");
+  }
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                 const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                 const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry points (no link to the driver
+// library); looked up once per process.
+EncodeTiled encoder() {
+  static EncodeTiled fn = []() -> EncodeTiled {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return reinterpret_cast<EncodeTiled>(f);
+  }();
+  return fn;
+}
+
+// A rows x dp FP16 matrix (row stride dp * 2 bytes, a multiple of 128) as TMA boxes of
+// 64 x 128 with 128-byte swizzling; rows past the end read as zeros.
+bool make_map(CUtensorMap* m, const __half* p, uint64_t rows, uint32_t dp) {
+  EncodeTiled enc = encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {dp, rows};
+  const cuuint64_t strides[1] = {static_cast<cuuint64_t>(dp) * 2};
+  const cuuint32_t box[2] = {kChunk, kRows};
+  const cuuint32_t elem[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<__half*>(p), dims, strides, box,
+             elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+uint32_t pick_mt(uint32_t kc, size_t smem_optin) {
+  return smem_bytes(2, kc) <= smem_optin ? 2u : 1u;
+}
+
+template <int MODE>
+cudaError_t launch(const CUtensorMap& ta, const CUtensorMap& tb, const Args& a, int num_sms,
+                   cudaStream_t st) {
+  const size_t smem = smem_bytes(a.mt, a.kc);
+  auto kern = k_gt_tc<MODE>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  const uint32_t q_tiles = (a.nq + kRows * a.mt - 1) / (kRows * a.mt);
+  const uint32_t grid = q_tiles < static_cast<uint32_t>(num_sms) ? q_tiles
+                                                                  : static_cast<uint32_t>(num_sms);
+  kern<<<grid ? grid : 1, kThreads, smem, st>>>(ta, tb, a);
+  return cudaGetLastError();
+}
+
+}  // namespace tc
+
 int blocks_for(uint64_t warps, int per_block, int num_sms, int per_sm) {
   uint64_t b = (warps + per_block - 1) / per_block;
   const uint64_t cap = static_cast<uint64_t>(num_sms) * per_sm;
@@ -523,56 +774,69 @@ int blocks_for(uint64_t warps, int per_block, int num_sms, int per_sm) {
   return static_cast<int>(b ? b : 1);
 }
 
+uint32_t padded_dim(uint32_t d) { return (d + tc::kChunk - 1) / tc::kChunk * tc::kChunk; }
+
 }  // namespace
 
 uint32_t gt_max_k() { return 256; }
 
-size_t gt_chunk_rows(uint64_t n, uint64_t nq) {
-  // an 8 GB score block: 2048 query rows per chunk at n = 1M (each chunk's GEMM re-reads the
-  // FP16 base, so larger chunks read it fewer times and give the GEMM a wider N)
-  uint64_t cq = (8ull << 30) / (4 * n);
-  if (cq < 1) cq = 1;
-  if (cq > 4096) cq = 4096;
+uint32_t gt_max_dim() { return tc::kChunk * tc::kMaxKc; }
+
+GtPlan gt_plan(uint64_t n, uint64_t nq, uint32_t d, int num_sms, size_t smem_optin) {
+  GtPlan p{};
+  p.dp = padded_dim(d);
+  p.kc = p.dp / tc::kChunk;
+  p.mt = tc::pick_mt(p.kc, smem_optin);
+  // groups of gs rows, as many as keep G >= 8192 groups (or one row per group for small n)
+  p.gs = 1;
+  while (p.gs < 4096 && n / (2ull * p.gs) >= 8192) p.gs *= 2;
+  p.groups = static_cast<uint32_t>((n + p.gs - 1) / p.gs);
+  // queries per chunk: whole waves of query tiles, the chunk's maxima and candidate lists
+  // within 4 GB
+  const uint64_t wave = static_cast<uint64_t>(tc::kRows) * p.mt * static_cast<uint64_t>(num_sms);
+  const uint64_t per_q = static_cast<uint64_t>(p.groups) * 4 + kGtCap * 8 + 16;
+  uint64_t cq = (4ull << 30) / per_q / wave * wave;
+  if (cq < static_cast<uint64_t>(tc::kRows) * p.mt) cq = static_cast<uint64_t>(tc::kRows) * p.mt;
   if (cq > nq) cq = nq;
-  return cq;
+  p.cq = cq;
+  return p;
 }
 
-size_t gt_workspace_bytes(uint64_t n, uint64_t nq, uint32_t d, uint32_t segs) {
-  const uint64_t cq = gt_chunk_rows(n, nq);
-  auto al = [](uint64_t b) { return (b + 255) & ~255ull; };
-  return al(n * d * 2) + al(nq * d * 2) + 2 * al(n * 4) + 2 * al(nq * 4) + al(8) + al(cq * 4) +
-         al(cq * n * 4) + al(cq * segs * kGtCap * 8) + al(cq * segs * 4) + al(cq * segs * 4);
+size_t gt_workspace_bytes(const GtPlan& p, uint64_t n, uint64_t nq) {
+  auto al = [](uint64_t b) { return (b + 1023) & ~1023ull; };
+  return al(n * p.dp * 2) + al(nq * p.dp * 2) + 2 * al(n * 4) + 2 * al(nq * 4) + al(8) +
+         2 * al(p.cq * 4) + al(p.cq * p.groups * 4) + al(p.cq * kGtCap * 8) + al(p.cq * 4);
 }
 
-int ground_truth(cublasContext* blas, const float* base, uint64_t n, uint32_t d,
+int ground_truth(const GtPlan& plan, const float* base, uint64_t n, uint32_t d,
                  const float* queries, uint64_t nq, uint32_t k, uint32_t* out, char* ws,
                  uint32_t* status, int num_sms, cudaStream_t st, float* diag) {
-  // segments per row (each keeps its own top k plus the margin in a kGtCap buffer)
-  const uint32_t kSegs = 8;
-  const uint64_t cq = gt_chunk_rows(n, nq);
-  auto al = [](uint64_t b) { return (b + 255) & ~255ull; };
+  const uint32_t dp = plan.dp;
+  const uint64_t cq = plan.cq;
+  auto al = [](uint64_t b) { return (b + 1023) & ~1023ull; };
   char* p = ws;
   auto take = [&](uint64_t bytes) {
     char* r = p;
     p += al(bytes);
     return r;
   };
-  __half* b16 = reinterpret_cast<__half*>(take(n * d * 2));
-  __half* q16 = reinterpret_cast<__half*>(take(nq * d * 2));
+  __half* b16 = reinterpret_cast<__half*>(take(n * dp * 2));
+  __half* q16 = reinterpret_cast<__half*>(take(nq * dp * 2));
   float* bn = reinterpret_cast<float*>(take(n * 4));
   float* be = reinterpret_cast<float*>(take(n * 4));
   float* qn = reinterpret_cast<float*>(take(nq * 4));
   float* qe = reinterpret_cast<float*>(take(nq * 4));
   uint32_t* xmax = reinterpret_cast<uint32_t*>(take(8));
   float* band = reinterpret_cast<float*>(take(cq * 4));
-  float* scores = reinterpret_cast<float*>(take(cq * n * 4));
-  uint64_t* seg_keys = reinterpret_cast<uint64_t*>(take(cq * kSegs * kGtCap * 8));
-  uint32_t* seg_cnt = reinterpret_cast<uint32_t*>(take(cq * kSegs * 4));
-  float* seg_theta = reinterpret_cast<float*>(take(cq * kSegs * 4));
+  float* lo = reinterpret_cast<float*>(take(cq * 4));
+  float* maxima = reinterpret_cast<float*>(take(cq * plan.groups * 4));
+  uint64_t* cand = reinterpret_cast<uint64_t*>(take(cq * kGtCap * 8));
+  uint32_t* cand_cnt = reinterpret_cast<uint32_t*>(take(cq * 4));
 
   cudaError_t e;
-  k_half_rows<<<blocks_for(n, 8, num_sms, 8), 256, 0, st>>>(base, n, d, b16, bn, be, status);
-  k_half_rows<<<blocks_for(nq, 8, num_sms, 8), 256, 0, st>>>(queries, nq, d, q16, qn, qe, status);
+  k_half_rows<<<blocks_for(n, 8, num_sms, 8), 256, 0, st>>>(base, n, d, dp, b16, bn, be, status);
+  k_half_rows<<<blocks_for(nq, 8, num_sms, 8), 256, 0, st>>>(queries, nq, d, dp, q16, qn, qe,
+                                                               status);
   if ((e = cudaMemsetAsync(xmax, 0, 8, st)) != cudaSuccess) return -static_cast<int>(e);
   {
     uint64_t g = (n + 255) / 256;
@@ -580,36 +844,42 @@ int ground_truth(cublasContext* blas, const float* base, uint64_t n, uint32_t d,
     k_max2<<<static_cast<unsigned>(g ? g : 1), 256, 0, st>>>(bn, be, n, xmax);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return -static_cast<int>(e);
-  if (cublasSetStream(blas, st) != CUBLAS_STATUS_SUCCESS) return 1;
-  const float one = 1.0f, zero = 0.0f;
+  CUtensorMap ta, tb;
+  if (!tc::make_map(&ta, q16, nq, dp) || !tc::make_map(&tb, b16, n, dp)) return 1;
   for (uint64_t q0 = 0; q0 < nq; q0 += cq) {
     const uint32_t rows = static_cast<uint32_t>(min(cq, nq - q0));
-    k_gt_band<<<(rows + 255) / 256, 256, 0, st>>>(qn + q0, qe + q0, xmax, rows, d, band);
-    // scores (column-major n x rows) = base16^T (n x d) . q16 (d x rows)
-    const cublasStatus_t bs = cublasGemmEx(
-        blas, CUBLAS_OP_T, CUBLAS_OP_N, static_cast<int>(n), static_cast<int>(rows),
-        static_cast<int>(d), &one, b16, CUDA_R_16F, static_cast<int>(d), q16 + q0 * d,
-        CUDA_R_16F, static_cast<int>(d), &zero, scores, CUDA_R_32F, static_cast<int>(n),
-        CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-    if (bs != CUBLAS_STATUS_SUCCESS) return 2;
-    GtArgs a{};
-    a.scores = scores;
-    a.n = n;
-    a.rows = rows;
-    a.k = k;
-    a.segs = kSegs;
-    a.band = band;
-    a.seg_keys = seg_keys;
-    a.seg_cnt = seg_cnt;
-    a.seg_theta = seg_theta;
-    a.base = base;
-    a.queries = queries + q0 * d;
-    a.d = d;
-    a.out = out + q0 * k;
+    k_gt_band<<<(rows + 255) / 256, 256, 0, st>>>(qn + q0, qe + q0, xmax, rows, dp, band);
+    tc::Args a{};
+    a.q0 = static_cast<uint32_t>(q0);
+    a.nq = rows;
+    a.n = static_cast<uint32_t>(n);
+    a.kc = plan.kc;
+    a.mt = plan.mt;
+    a.gs = plan.gs;
+    a.groups = plan.groups;
+    a.maxima = maxima;
+    a.lo = lo;
+    a.cand = cand;
+    a.cand_cnt = cand_cnt;
     a.status = status;
-    k_gt_scan<<<blocks_for(static_cast<uint64_t>(rows) * kSegs, kScanWarps, num_sms, 16),
-                kScanWarps * 32, 0, st>>>(a);
-    k_gt_final<<<blocks_for(rows, kFinalWarps, num_sms, 16), kFinalWarps * 32, 0, st>>>(a);
+    if ((e = tc::launch<tc::kMax>(ta, tb, a, num_sms, st)) != cudaSuccess)
+      return -static_cast<int>(e);
+    k_gt_theta<<<blocks_for(rows, 8, num_sms, 8), 256, 0, st>>>(maxima, rows, plan.groups, k,
+                                                                band, lo);
+    if ((e = tc::launch<tc::kFilter>(ta, tb, a, num_sms, st)) != cudaSuccess)
+      return -static_cast<int>(e);
+    GtArgs f{};
+    f.base = base;
+    f.queries = queries + q0 * d;
+    f.d = d;
+    f.k = k;
+    f.rows = rows;
+    f.cand = cand;
+    f.cand_cnt = cand_cnt;
+    f.band = band;
+    f.out = out + q0 * k;
+    f.status = status;
+    k_gt_final<<<blocks_for(rows, kFinalWarps, num_sms, 16), kFinalWarps * 32, 0, st>>>(f);
     if ((e = cudaGetLastError()) != cudaSuccess) return -static_cast<int>(e);
     if (diag && q0 == 0) {  // the first query's margin and the base's largest norms
       if ((e = cudaMemcpyAsync(diag, band, 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
@@ -619,6 +889,49 @@ int ground_truth(cublasContext* blas, const float* base, uint64_t n, uint32_t d,
     }
   }
   return 0;
+}
+
+size_t screen_scores_workspace(uint64_t na, uint64_t nb, uint32_t d) {
+  auto al = [](uint64_t b) { return (b + 1023) & ~1023ull; };
+  const uint32_t dp = padded_dim(d);
+  return al(na * dp * 2) + al(nb * dp * 2) + 2 * al(na * 4) + 2 * al(nb * 4);
+}
+
+int screen_scores(const float* a, uint64_t na, const float* b, uint64_t nb, uint32_t d,
+                  float* out, char* ws, uint32_t* status, int num_sms, size_t smem_optin,
+                  cudaStream_t st) {
+  const uint32_t dp = padded_dim(d);
+  auto al = [](uint64_t x) { return (x + 1023) & ~1023ull; };
+  char* p = ws;
+  auto take = [&](uint64_t bytes) {
+    char* r = p;
+    p += al(bytes);
+    return r;
+  };
+  __half* a16 = reinterpret_cast<__half*>(take(na * dp * 2));
+  __half* b16 = reinterpret_cast<__half*>(take(nb * dp * 2));
+  float* an = reinterpret_cast<float*>(take(na * 4));
+  float* ae = reinterpret_cast<float*>(take(na * 4));
+  float* bn = reinterpret_cast<float*>(take(nb * 4));
+  float* be = reinterpret_cast<float*>(take(nb * 4));
+  k_half_rows<<<blocks_for(na, 8, num_sms, 8), 256, 0, st>>>(a, na, d, dp, a16, an, ae, status);
+  k_half_rows<<<blocks_for(nb, 8, num_sms, 8), 256, 0, st>>>(b, nb, d, dp, b16, bn, be, status);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return -static_cast<int>(e);
+  CUtensorMap ta, tb;
+  if (!tc::make_map(&ta, a16, na, dp) || !tc::make_map(&tb, b16, nb, dp)) return 1;
+  tc::Args x{};
+  x.q0 = 0;
+  x.nq = static_cast<uint32_t>(na);
+  x.n = static_cast<uint32_t>(nb);
+  x.kc = dp / tc::kChunk;
+  x.mt = tc::pick_mt(x.kc, smem_optin);
+  x.gs = 1;
+  x.groups = 1;
+  x.dump = out;
+  x.status = status;
+  e = tc::launch<tc::kDump>(ta, tb, x, num_sms, st);
+  return e == cudaSuccess ? 0 : -static_cast<int>(e);
 }
 
 }  // namespace pg

@@ -3,8 +3,6 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-struct cublasContext;  // cublasHandle_t
-
 namespace pg {
 
 struct PruneArgs {
@@ -139,14 +137,33 @@ cudaError_t launch_sup_merge(const SupArgs& a, int num_sms, cudaStream_t st);
 cudaError_t launch_fusion_nn(const FusionArgs& a, int num_sms, cudaStream_t st);
 cudaError_t launch_fusion_final(const FusionArgs& a, int num_sms, cudaStream_t st);
 
-// Exact inner-product top-k ground truth (pg_gt.cu).  Returns 0, a negative cudaError_t, or a
-// positive code for a cuBLAS failure; device-side overflow sets kErrCapacity in *status.
+// Exact inner-product top-k ground truth (pg_gt.cu): FP16 screening on the tensor cores
+// (tcgen05) with a rigorous margin, FP64 re-ranking.  gt_plan picks the padded dimension, the
+// M tiles per CTA, the group size of the threshold pass and the queries per chunk.  The entry
+// points return 0, a negative cudaError_t, or 1 when a TMA tensor map cannot be encoded;
+// device-side problems set bits in *status (1 << 4: a value beyond the FP16 range, 1 << 6: a
+// query with more candidates than the selection holds, kErrWait: a bounded wait gave up).
+struct GtPlan {
+  uint32_t dp;      // d rounded up to a multiple of 64 (FP16 rows zero-padded)
+  uint32_t kc;      // dp / 64
+  uint32_t mt;      // 128-row M tiles per CTA (1 or 2)
+  uint32_t gs;      // base rows per group of the threshold pass
+  uint32_t groups;  // ceil(n / gs)
+  uint64_t cq;      // queries per chunk
+};
 uint32_t gt_max_k();
-size_t gt_chunk_rows(uint64_t n, uint64_t nq);
-size_t gt_workspace_bytes(uint64_t n, uint64_t nq, uint32_t d, uint32_t segs);
-int ground_truth(cublasContext* blas, const float* base, uint64_t n, uint32_t d,
+uint32_t gt_max_dim();
+GtPlan gt_plan(uint64_t n, uint64_t nq, uint32_t d, int num_sms, size_t smem_optin);
+size_t gt_workspace_bytes(const GtPlan& p, uint64_t n, uint64_t nq);
+int ground_truth(const GtPlan& plan, const float* base, uint64_t n, uint32_t d,
                  const float* queries, uint64_t nq, uint32_t k, uint32_t* out, char* ws,
                  uint32_t* status, int num_sms, cudaStream_t st, float* diag = nullptr);
+// out (na x nb, FP32) = fp16(a) . fp16(b)^T accumulated in FP32 on the tensor cores: the
+// screening product of ground_truth on its own.
+size_t screen_scores_workspace(uint64_t na, uint64_t nb, uint32_t d);
+int screen_scores(const float* a, uint64_t na, const float* b, uint64_t nb, uint32_t d,
+                  float* out, char* ws, uint32_t* status, int num_sms, size_t smem_optin,
+                  cudaStream_t st);
 
 cudaError_t launch_match_winner(const uint32_t* gt, uint64_t q, uint32_t gt_k, uint64_t n,
                                 uint32_t* winner, uint32_t* status, int num_sms, cudaStream_t st,

@@ -1,4 +1,5 @@
-"""Full-size parity: the 1M x 200 inner-product build (M=32, L=64) against the oracle.
+"""Full-size parity: the 1M x 200 inner-product build (M=32, L=64) and the 1M x 512 cosine build
+(M=48, L=96) against the oracle.
 
 The oracle builds the same 1M-point graph on the host cores in seconds, so the benchmark's own
 workload is checked id for id (projection, final graph, evaluation counts), and two GPU builds
@@ -97,3 +98,44 @@ def test_full_size_index_matches_oracle(workload):
     assert np.array_equal(k, ref_k), f"{(k != ref_k).sum()} row lengths differ"
     mask = np.arange(rows.shape[1])[None, :] < k[:, None]
     assert np.array_equal(rows[mask], ids), "index ids differ"
+
+
+def test_full_size_cosine_512_screened_equals_plain_and_oracle():
+    """The precision configuration at full size: 1M x 512, base and queries L2-normalised
+    (cosine), 128 centres, M = 48, L = 96 (Km = 64), ground truth top-128 from pg_ground_truth.
+    The FP16-screened build, the plain FP32 build and the oracle give the same projection, graph
+    and evaluation counts."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import paragraph_gb300 as pg
+    from paragraph_gb300 import datagen
+    n, d = 1_000_000, 512
+    base, _, queries = datagen.make_dataset_cuda(n, d, cosine=True, centers=128, seed=4321,
+                                                 device="cuda", with_gt=False)
+    gt = torch.empty((n, 128), dtype=torch.int32, device="cuda")
+    outs, stats = [], []
+    with pg.Handle(0) as h:
+        h.ground_truth(base, queries, gt)
+        del queries
+        torch.cuda.empty_cache()
+        for screen in (pg.SCREEN_FP16, pg.SCREEN_NONE):
+            graph = torch.empty((n, 48), dtype=torch.int32, device="cuda")
+            proj = torch.empty((n, 16), dtype=torch.int32, device="cuda")
+            stats.append(h.build_device(base, gt, graph, proj,
+                                        pg.default_params(48, 96, screen=screen)))
+            outs.append((graph.cpu().numpy().view(np.uint32), proj.cpu().numpy().view(np.uint32)))
+    assert np.array_equal(outs[0][1], outs[1][1]), "projection: screened != plain"
+    bad = (outs[0][0] != outs[1][0]).any(axis=1)
+    assert not bad.any(), f"{bad.sum()} rows differ between the screened and the plain build"
+    assert stats[0].evals_total == stats[1].evals_total
+    base_np = base.cpu().numpy()
+    gt_np = gt.cpu().numpy().view(np.uint32)
+    del base, gt
+    torch.cuda.empty_cache()
+    ref = oracle.build_graph(base_np, gt_np, degree=48, beam=96)
+    assert np.array_equal(outs[1][1], ref["proj"])
+    bad = (outs[1][0] != ref["graph"]).any(axis=1)
+    assert not bad.any(), f"{bad.sum()} of {n} graph rows differ from the oracle"
+    assert stats[1].evals_total == ref["stats"]["evals_total"]
+    print(f"cosine 1M x 512: screened {stats[0].ms_total:.1f} ms, plain {stats[1].ms_total:.1f} ms,"
+          f" rescored {list(stats[0].rescored)[:2]}")
