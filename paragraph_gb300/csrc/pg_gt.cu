@@ -5,29 +5,29 @@
 // k base ids with the largest FP64 inner product q.x, ties to the lower id -- exact, whatever the
 // arithmetic used to find them.
 //
-//   1. FP16 copies of base and queries, rows zero-padded to a multiple of 64 elements, with
+//   1. FP16 copies of base and queries, rows zero-padded to a multiple of 16 elements, with
 //      per-row norms |x^| and |x - x^| (k_half_rows);
 //   2. screening scores s^ = q^.x^ on the tensor cores: k_gt_tc, a persistent tcgen05 GEMM
 //      (TMA-loaded 128-byte-swizzled tiles, FP32 accumulators in TMEM) whose epilogue consumes
-//      each 128 x 128 tile of scores in registers -- no score matrix is ever stored;
+//      each tile of scores in registers -- no score matrix is ever stored;
 //   3. a rigorous bound: |q.x - s^| <= E_q = (|q^| + |e_q|) max|e_x| + |e_q| max|x^|
 //      + g (|q^| max|x^|), with g covering the FP32 accumulation (d' * 2^-22, four times the
 //      IEEE unit roundoff, for the tensor core's accumulation);
-//   4. pass 1 (k_gt_tc<kMax>): the maximum screened score of every group of gs consecutive base
-//      rows per query; the k-th largest group maximum theta_q is the score of k distinct base
-//      rows, so theta_q <= t_k, the k-th largest screened score of the row (k_gt_theta);
+//   4. pass 1 (k_gt_tc<kMax>): the maximum screened score of every group of base rows per query
+//      (disjoint groups, about 4096 or more of them); the k-th largest group maximum theta_q is
+//      the score of k distinct base rows, so theta_q <= t_k, the k-th largest screened score of
+//      the row (k_gt_theta);
 //   5. pass 2 (k_gt_tc<kFilter>): every base row with s^ >= theta_q - 2 E_q is a candidate --
 //      a superset of {s^ >= t_k - 2 E_q}, which holds the true top k (a true top-k member has
 //      s^ >= s_k - E_q and s_k >= t_k - E_q);
 //   6. k_gt_final: the candidates with s^ >= t_k - 2 E_q, exact FP64 inner products, sorted by
 //      (score desc, id asc).
-// With groups small enough that the top k fall in distinct groups (G = n / gs >= 8192 where n
-// allows), theta_q sits just below t_k and a query keeps about 1.1 k candidates.
+// With groups many enough that the top k fall in nearly distinct groups, theta_q sits just
+// below t_k and a query keeps about 1.1 k candidates.
 #include <cuda.h>
 #include <cuda_fp16.h>
 
 #include <cmath>
-#include <mutex>
 
 #include "pg_device.cuh"
 #include "pg_kernels.h"
@@ -231,8 +231,8 @@ struct GtArgs {
   const float* queries;  // rows x d (FP32, this chunk)
   uint32_t d, k;
   uint32_t rows;
-  const uint64_t* cand;      // rows x kGtCap keys (desc_key)
-  const uint32_t* cand_cnt;  // rows
+  const uint64_t* cand;      // rows x kGtCap keys (desc_key), two halves of kGtCap / 2
+  const uint32_t* cand_cnt;  // rows x 2
   const float* band;         // rows
   uint32_t* out;             // rows x k
   uint32_t* status;
@@ -316,9 +316,13 @@ __global__ void __launch_bounds__(kFinalWarps * 32) k_gt_final(GtArgs a) {
   const uint64_t nw = static_cast<uint64_t>(gridDim.x) * kFinalWarps;
   for (uint64_t row = blockIdx.x * static_cast<uint64_t>(kFinalWarps) + (threadIdx.x >> 5);
        row < a.rows; row += nw) {
-    uint32_t cnt = min(a.cand_cnt[row], kGtCap);
+    // the row's list is two halves of kGtCap / 2, one per half of the columns
+    const uint32_t c0 = min(a.cand_cnt[2 * row], kGtCap / 2);
+    const uint32_t c1 = min(a.cand_cnt[2 * row + 1], kGtCap / 2);
     const uint64_t* src = a.cand + row * kGtCap;
-    for (uint32_t i = lane; i < cnt; i += 32) buf[i] = src[i];
+    for (uint32_t i = lane; i < c0; i += 32) buf[i] = src[i];
+    for (uint32_t i = lane; i < c1; i += 32) buf[c0 + i] = src[kGtCap / 2 + i];
+    uint32_t cnt = c0 + c1;
     __syncwarp();
     compact_any(buf, cnt, a.k, a.band[row]);  // candidates >= t_k - band, sorted
     if (cnt <= 128)
@@ -356,29 +360,37 @@ __global__ void __launch_bounds__(256) k_gt_theta(const float* __restrict__ maxi
 
 // ---------------------------------------------------------------- tcgen05 screening GEMM
 //
-// D (128 queries x 128 base rows, FP32 in TMEM) = A (queries, FP16, K-major) . B (base rows,
-// FP16, K-major)^T, K = dp in boxes of 64 elements (one 128-byte swizzled row per box row).
-// One CTA per SM, persistent over query tiles of 128 * mt rows (mt = 1 or 2 M tiles sharing each
-// B tile); for each query tile it sweeps every base tile in order:
-//   warp 0      TMA producer: A tiles once per query tile, B boxes through a kStages ring;
-//   warp 1      TMEM owner and MMA issuer (one thread): 4 MMAs (K = 16) per box per M tile,
+// D (128 queries x BN base rows, FP32 in TMEM) = A (queries, FP16, K-major) . B (base rows,
+// FP16, K-major)^T, K = dp in boxes of 64 elements (one 128-byte swizzled row per box row; the
+// last box's columns past dp are read as zeros and its MMA K steps past dp are not issued).
+// One CTA per SM, persistent over query tiles of 128 * MT rows (MT = 256 / BN M tiles sharing
+// each B tile); for each query tile it sweeps every base tile in order:
+//   warp 0      TMA producer: A tiles once per query tile, B boxes through a ring of stages;
+//   warp 1      TMEM owner and MMA issuer (one thread): 4 MMAs (K = 16) per K box per M tile,
 //               into one of two accumulator buffers per M tile;
-//   warps 2..5  epilogue: TMEM -> registers (warp w reads TMEM lanes 32 (w % 4) ..), one thread
-//               per query row, the mode's work on 128 scores per M tile, then the buffer is
-//               released.
+//   warps 2..9  epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (one thread per query row)
+//               and half of each tile's columns; each thread takes 128 scores per tile (4 chunks
+//               of 32) with one TMEM wait, does the mode's work in straight-line code, then
+//               releases the buffer.
 // Every wait is bounded (1 s); a wait that gives up raises kErrWait, the CTA's roles stop, the
 // issued MMAs are drained and the TMEM is freed before the CTA exits.
 namespace tc {
 
-constexpr uint32_t kRows = 128;  // rows of an A tile (queries) and of a B tile (base rows)
+constexpr uint32_t kRows = 128;  // rows of an A tile (queries) and of a TMA box
 constexpr uint32_t kChunk = 64;  // K elements per TMA box
 constexpr uint32_t kBox = kRows * kChunk * 2;  // 16 KB
-constexpr uint32_t kStages = 5;
-constexpr uint32_t kThreads = 192;
+constexpr uint32_t kEpiWarps = 8;
+constexpr uint32_t kThreads = 64 + 32 * kEpiWarps;
 constexpr uint32_t kMaxKc = 8;  // dp <= 512
+constexpr uint32_t kMinStages = 3, kMaxStages = 6;
+constexpr uint32_t kHalfCap = kGtCap / 2;  // candidates per (query row, half of the columns)
+
 // kind::f16 instruction descriptor: FP32 accumulator (bits 4-5 = 1), A and B FP16 (0), both
 // K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t kIdesc = (1u << 4) | ((kRows >> 3) << 17) | ((kRows >> 4) << 24);
+template <uint32_t BN>
+constexpr uint32_t idesc() {
+  return (1u << 4) | ((BN >> 3) << 17) | ((kRows >> 4) << 24);
+}
 
 enum Mode : int { kMax = 0, kFilter = 1, kDump = 2 };
 
@@ -386,14 +398,17 @@ struct Args {
   uint32_t q0;      // first row of this chunk in the query tensor map
   uint32_t nq;      // query rows of this chunk
   uint32_t n;       // base rows
-  uint32_t kc;      // K boxes per row: dp / 64
-  uint32_t mt;      // M tiles per query tile (1 or 2)
-  uint32_t gs;      // kMax: group size (power of two)
-  uint32_t groups;  // kMax: ceil(n / gs)
+  uint32_t kc;      // K boxes per row: ceil(dp / 64)
+  uint32_t klast;   // MMA K steps (of 16) in the last box: 1 .. 4
+  uint32_t stages;  // B ring stages
+  // kMax: groups of base rows whose maxima are stored (groups per query row).  span > 0: a
+  // group is `span` consecutive 32-column chunks of one thread (one half of each tile); span
+  // == 0: a group is gs consecutive columns (gs < 32, for small n).
+  uint32_t span, gs, groups;
   float* maxima;    // kMax: nq x groups
   const float* lo;  // kFilter: nq thresholds
-  uint64_t* cand;   // kFilter: nq x kGtCap keys
-  uint32_t* cand_cnt;  // kFilter: nq
+  uint64_t* cand;   // kFilter: nq x kGtCap keys, two halves of kGtCap / 2
+  uint32_t* cand_cnt;  // kFilter: nq x 2 (one count per half)
   float* dump;      // kDump: nq x n scores
   uint32_t* status;
 };
@@ -458,11 +473,12 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
   return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) | (static_cast<uint64_t>(1024 >> 4) << 32) |
          (1ull << 46) | (2ull << 61);
 }
+template <uint32_t BN>
 __device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+      "l"(a), "l"(b), "r"(idesc<BN>()), "r"(acc)
       : "memory");
 }
 __device__ __forceinline__ void commit(uint64_t* bar) {
@@ -477,8 +493,8 @@ __device__ __forceinline__ void fence_before() {
 __device__ __forceinline__ void fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
-// 32 consecutive FP32 columns of this thread's TMEM lane.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+// 32 consecutive FP32 columns of this thread's TMEM lane into v[0..31] (no wait).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
       "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
@@ -489,24 +505,50 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
         "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
         "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
       : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-size_t smem_bytes(uint32_t mt, uint32_t kc) {
-  return 1024 + static_cast<size_t>(mt) * kc * kBox + kStages * kBox + 256;
+__device__ __forceinline__ float max32(const uint32_t* v) {  // pairwise tree, 31 FMNMX
+  float m[16];
+#pragma unroll
+  for (int j = 0; j < 16; j++) m[j] = fmaxf(__uint_as_float(v[j]), __uint_as_float(v[j + 16]));
+#pragma unroll
+  for (int w = 8; w >= 1; w >>= 1)
+#pragma unroll
+    for (int j = 0; j < w; j++) m[j] = fmaxf(m[j], m[j + w]);
+  return m[0];
 }
 
-template <int MODE>
+// Bits j of the 32 columns col0 + j that are < n.
+__device__ __forceinline__ uint32_t in_range(uint32_t col0, uint32_t n) {
+  if (col0 + 32 <= n) return 0xFFFFFFFFu;
+  return col0 >= n ? 0u : ((1u << (n - col0)) - 1u);
+}
+
+template <uint32_t BN>
+size_t smem_bytes(uint32_t kc, uint32_t stages) {
+  constexpr uint32_t MT = 256 / BN;
+  return 1024 + static_cast<size_t>(MT) * kc * kBox + static_cast<size_t>(stages) * BN * 128 + 256;
+}
+
+template <int MODE, uint32_t BN>
 __global__ void __launch_bounds__(kThreads, 1)
     k_gt_tc(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
             const Args a) {
+  constexpr uint32_t MT = 256 / BN;           // M tiles per query tile
+  constexpr uint32_t kStageBytes = BN * 128;  // BN rows x 64 K x 2 bytes
+  constexpr uint32_t kHalf = BN / 2;          // columns per epilogue thread per tile
+  constexpr uint32_t kCpt = kHalf / 32;       // chunks per thread per tile and M tile
+  static_assert(MT * kCpt == 4, "four 32-column chunks per thread per tile");
   extern __shared__ __align__(16) uint8_t smem_raw[];
   uint8_t* sm = smem_raw + ((1024u - (saddr(smem_raw) & 1023u)) & 1023u);
-  uint8_t* sA = sm;  // mt x kc boxes
-  uint8_t* sB = sA + static_cast<size_t>(a.mt) * a.kc * kBox;  // kStages boxes
-  uint64_t* full = reinterpret_cast<uint64_t*>(sB + kStages * kBox);
-  uint64_t* empty = full + kStages;
-  uint64_t* a_full = empty + kStages;
+  uint8_t* sA = sm;                                       // MT x kc boxes
+  uint8_t* sB = sA + static_cast<size_t>(MT) * a.kc * kBox;  // stages x (BN rows x 128 bytes)
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + static_cast<size_t>(a.stages) * kStageBytes);
+  uint64_t* empty = full + a.stages;
+  uint64_t* a_full = empty + a.stages;
   uint64_t* a_empty = a_full + 1;
   uint64_t* t_full = a_empty + 1;   // [2]
   uint64_t* t_empty = t_full + 2;   // [2]
@@ -515,13 +557,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   volatile uint32_t* stop = tmem_slot + 1;
 
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint32_t rows_per_tile = kRows * a.mt;
+  constexpr uint32_t rows_per_tile = kRows * MT;
   const uint32_t q_tiles = (a.nq + rows_per_tile - 1) / rows_per_tile;
-  const uint32_t n_tiles = (a.n + kRows - 1) / kRows;
-  const uint32_t ncols = 256u * a.mt;  // two accumulator buffers of 128 columns per M tile
+  const uint32_t n_tiles = (a.n + BN - 1) / BN;
+  constexpr uint32_t ncols = 2 * BN * MT;  // two accumulator buffers per M tile (512)
 
   if (threadIdx.x == 0) {
-    for (uint32_t s = 0; s < kStages; s++) {
+    for (uint32_t s = 0; s < a.stages; s++) {
       bar_init(full + s, 1);
       bar_init(empty + s, 1);
     }
@@ -529,7 +571,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     bar_init(a_empty, 1);
     for (int b = 0; b < 2; b++) {
       bar_init(t_full + b, 1);
-      bar_init(t_empty + b, kRows);
+      bar_init(t_empty + b, 32 * kEpiWarps);
     }
     bar_init(drained, 1);
     *stop = 0;
@@ -558,20 +600,23 @@ __global__ void __launch_bounds__(kThreads, 1)
           ok = false;
           break;
         }
-        bar_expect_tx(a_full, a.mt * a.kc * kBox);
-        for (uint32_t m = 0; m < a.mt; m++)
+        bar_expect_tx(a_full, MT * a.kc * kBox);
+        for (uint32_t m = 0; m < MT; m++)
           for (uint32_t c = 0; c < a.kc; c++)
             tma_load(sA + (m * a.kc + c) * kBox, &ta, c * kChunk,
                      a.q0 + st * rows_per_tile + m * kRows, a_full);
         for (uint32_t bt = 0; ok && bt < n_tiles; bt++)
           for (uint32_t c = 0; c < a.kc; c++, it++) {
-            const uint32_t s = it % kStages, ph = (it / kStages) & 1u;
+            const uint32_t s = it % a.stages, ph = (it / a.stages) & 1u;
             if (!bar_wait(empty + s, ph ^ 1u, stop)) {
               ok = false;
               break;
             }
-            bar_expect_tx(full + s, kBox);
-            tma_load(sB + s * kBox, &tb, c * kChunk, bt * kRows, full + s);
+            bar_expect_tx(full + s, kStageBytes);
+#pragma unroll
+            for (uint32_t r = 0; r < BN / kRows; r++)
+              tma_load(sB + s * kStageBytes + r * kBox, &tb, c * kChunk, bt * BN + r * kRows,
+                       full + s);
           }
       }
       if (!ok) {
@@ -579,9 +624,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         *stop = 1;
       }
       // the loads still in flight land before the CTA exits: each stage's last issued load
-      for (uint32_t j = 0; j < kStages && j < it; j++) {
+      for (uint32_t j = 0; j < a.stages && j < it; j++) {
         const uint32_t i = it - 1 - j;
-        bar_wait(full + (i % kStages), (i / kStages) & 1u, nullptr);
+        bar_wait(full + (i % a.stages), (i / a.stages) & 1u, nullptr);
       }
     }
   } else if (warp == 1) {
@@ -604,17 +649,21 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           fence_after();
           for (uint32_t c = 0; c < a.kc; c++, it++) {
-            const uint32_t s = it % kStages, ph = (it / kStages) & 1u;
+            const uint32_t s = it % a.stages, ph = (it / a.stages) & 1u;
             if (!bar_wait(full + s, ph, stop)) {
               ok = false;
               break;
             }
             fence_after();
-            for (uint32_t m = 0; m < a.mt; m++)
+            const uint32_t ks = c + 1 == a.kc ? a.klast : 4u;  // zero columns past dp skipped
+#pragma unroll
+            for (uint32_t m = 0; m < MT; m++)
 #pragma unroll
               for (uint32_t k = 0; k < 4; k++)
-                mma(tmem + (m * 2 + buf) * kRows, sw128_desc(a0 + (m * a.kc + c) * kBox + k * 32),
-                    sw128_desc(b0 + s * kBox + k * 32), (c | k) != 0);
+                if (k < ks)
+                  mma<BN>(tmem + (m * 2 + buf) * BN,
+                          sw128_desc(a0 + (m * a.kc + c) * kBox + k * 32),
+                          sw128_desc(b0 + s * kStageBytes + k * 32), (c | k) != 0);
             commit(empty + s);  // the stage is free once these MMAs have read it
           }
           if (ok) commit(t_full + buf);
@@ -629,73 +678,107 @@ __global__ void __launch_bounds__(kThreads, 1)
       bar_wait(drained, 0, nullptr);
     }
   } else {
-    // ---- epilogue: one thread per query row of each M tile
+    // ---- epilogue: one thread per (query row, half of the tile's columns)
     const uint32_t quarter = warp & 3u;
+    const uint32_t half = (warp - 2) >> 2;
     const uint32_t row = quarter * 32u + lane;
     const uint32_t lane_base = (quarter * 32u) << 16;
     bool ok = true;
     uint32_t t = 0;
+    const uint32_t chunks = n_tiles * kCpt;  // this thread's 32-column chunks per M tile
     for (uint32_t st = blockIdx.x; ok && st < q_tiles; st += gridDim.x) {
-      uint32_t qrow[2], cnt[2] = {0, 0};
-      bool valid[2];
-      float lo[2], gmax[2] = {-INFINITY, -INFINITY};
-      for (uint32_t m = 0; m < 2; m++) {
+      uint32_t qrow[MT], cnt[MT];
+      bool valid[MT];
+      float lo[MT], run[MT];
+#pragma unroll
+      for (uint32_t m = 0; m < MT; m++) {
         qrow[m] = st * rows_per_tile + m * kRows + row;
-        valid[m] = m < a.mt && qrow[m] < a.nq;
+        valid[m] = qrow[m] < a.nq;
         lo[m] = (MODE == kFilter && valid[m]) ? a.lo[qrow[m]] : INFINITY;
+        run[m] = -INFINITY;
+        cnt[m] = 0;
       }
       for (uint32_t bt = 0; bt < n_tiles; bt++, t++) {
         const uint32_t buf = t & 1u, use = t >> 1;
         ok = __all_sync(kFull, bar_wait(t_full + buf, use & 1u, stop));
         if (!ok) break;
         fence_after();
-        for (uint32_t m = 0; m < a.mt; m++) {
-#pragma unroll 1
-          for (uint32_t ch = 0; ch < 4; ch++) {
-            uint32_t v[32];
-            tmem_ld32(tmem + lane_base + (m * 2 + buf) * kRows + ch * 32, v);
-            if (!valid[m]) continue;
-            const uint32_t col0 = bt * kRows + ch * 32;
-            if (MODE == kMax) {
+        uint32_t v[4][32];
+#pragma unroll
+        for (uint32_t i = 0; i < 4; i++) {
+          const uint32_t m = i / kCpt, ch = i % kCpt;
+          tmem_ld32(tmem + lane_base + (m * 2 + buf) * BN + half * kHalf + ch * 32, v[i]);
+        }
+        tmem_wait_ld();
+        fence_before();
+        bar_arrive(t_empty + buf);  // the scores are in registers: the buffer is free
+#pragma unroll
+        for (uint32_t i = 0; i < 4; i++) {
+          const uint32_t m = i / kCpt, ch = i % kCpt;
+          if (!valid[m]) continue;
+          const uint32_t col0 = bt * BN + half * kHalf + ch * 32;
+          const uint32_t inr = in_range(col0, a.n);
+          if (MODE == kMax) {
+            if (a.span) {
+              float mx = max32(v[i]);
+              if (inr != 0xFFFFFFFFu) {  // the last tile: only columns < n count
+                mx = -INFINITY;
+#pragma unroll
+                for (uint32_t j = 0; j < 32; j++)
+                  if ((inr >> j) & 1u) mx = fmaxf(mx, __uint_as_float(v[i][j]));
+              }
+              run[m] = fmaxf(run[m], mx);
+              const uint32_t u = bt * kCpt + ch;  // this thread's chunk index
+              if (((u + 1) & (a.span - 1)) == 0 || u + 1 == chunks) {
+                a.maxima[static_cast<uint64_t>(qrow[m]) * a.groups + (u / a.span) * 2 + half] =
+                    run[m];
+                run[m] = -INFINITY;
+              }
+            } else {  // small n: groups of gs < 32 columns
 #pragma unroll
               for (uint32_t j = 0; j < 32; j++) {
                 const uint32_t c = col0 + j;
-                if (c < a.n) {
-                  gmax[m] = fmaxf(gmax[m], __uint_as_float(v[j]));
+                if ((inr >> j) & 1u) {
+                  run[m] = fmaxf(run[m], __uint_as_float(v[i][j]));
                   if (((c + 1) & (a.gs - 1)) == 0 || c + 1 == a.n) {
-                    a.maxima[static_cast<uint64_t>(qrow[m]) * a.groups + c / a.gs] = gmax[m];
-                    gmax[m] = -INFINITY;
+                    a.maxima[static_cast<uint64_t>(qrow[m]) * a.groups + c / a.gs] = run[m];
+                    run[m] = -INFINITY;
                   }
                 }
               }
-            } else if (MODE == kFilter) {
+            }
+          } else if (MODE == kFilter) {
+            uint32_t hit = 0;
 #pragma unroll
-              for (uint32_t j = 0; j < 32; j++) {
-                const uint32_t c = col0 + j;
-                const float x = __uint_as_float(v[j]);
-                if (c < a.n && x >= lo[m]) {
-                  if (cnt[m] < kGtCap)
-                    a.cand[static_cast<uint64_t>(qrow[m]) * kGtCap + cnt[m]] = desc_key(x, c);
-                  cnt[m]++;
-                }
-              }
-            } else {
-              float* o = a.dump + static_cast<uint64_t>(qrow[m]) * a.n;
+            for (uint32_t j = 0; j < 32; j++)
+              hit |= (__uint_as_float(v[i][j]) >= lo[m]) ? (1u << j) : 0u;
+            hit &= inr;
+            if (hit) {
+              uint64_t* dst = a.cand + static_cast<uint64_t>(qrow[m]) * kGtCap + half * kHalfCap;
 #pragma unroll
               for (uint32_t j = 0; j < 32; j++)
-                if (col0 + j < a.n) o[col0 + j] = __uint_as_float(v[j]);
+                if ((hit >> j) & 1u) {
+                  if (cnt[m] < kHalfCap) dst[cnt[m]] = desc_key(__uint_as_float(v[i][j]), col0 + j);
+                  cnt[m]++;
+                }
             }
+          } else {
+            float* o = a.dump + static_cast<uint64_t>(qrow[m]) * a.n;
+#pragma unroll
+            for (uint32_t j = 0; j < 32; j++)
+              if ((inr >> j) & 1u) o[col0 + j] = __uint_as_float(v[i][j]);
           }
         }
-        fence_before();
-        bar_arrive(t_empty + buf);
       }
-      if (MODE == kFilter && ok)
-        for (uint32_t m = 0; m < a.mt; m++)
+      if (MODE == kFilter && ok) {
+        // each half of a row keeps its candidates in its own half of the row's list
+#pragma unroll
+        for (uint32_t m = 0; m < MT; m++)
           if (valid[m]) {
-            a.cand_cnt[qrow[m]] = min(cnt[m], kGtCap);
-            if (cnt[m] > kGtCap) raise_error(a.status, kGtErrFinal);
+            a.cand_cnt[static_cast<uint64_t>(qrow[m]) * 2 + half] = min(cnt[m], kHalfCap);
+            if (cnt[m] > kHalfCap) raise_error(a.status, kGtErrFinal);
           }
+      }
     }
     if (!ok && lane == 0) {
       raise_error(a.status, kErrWait);
@@ -732,8 +815,8 @@ EncodeTiled encoder() {
   return fn;
 }
 
-// A rows x dp FP16 matrix (row stride dp * 2 bytes, a multiple of 128) as TMA boxes of
-// 64 x 128 with 128-byte swizzling; rows past the end read as zeros.
+// A rows x dp FP16 matrix (row stride dp * 2 bytes, a multiple of 32) as TMA boxes of
+// 64 x 128 with 128-byte swizzling; rows and columns past the end read as zeros.
 bool make_map(CUtensorMap* m, const __half* p, uint64_t rows, uint32_t dp) {
   EncodeTiled enc = encoder();
   if (!enc) return false;
@@ -746,23 +829,37 @@ bool make_map(CUtensorMap* m, const __half* p, uint64_t rows, uint32_t dp) {
              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-uint32_t pick_mt(uint32_t kc, size_t smem_optin) {
-  return smem_bytes(2, kc) <= smem_optin ? 2u : 1u;
+template <uint32_t BN>
+uint32_t stages_for(uint32_t kc, size_t smem_optin) {
+  uint32_t s = kMaxStages;
+  while (s > kMinStages && smem_bytes<BN>(kc, s) > smem_optin) s--;
+  return smem_bytes<BN>(kc, s) <= smem_optin ? s : 0;
 }
 
-template <int MODE>
-cudaError_t launch(const CUtensorMap& ta, const CUtensorMap& tb, const Args& a, int num_sms,
-                   cudaStream_t st) {
-  const size_t smem = smem_bytes(a.mt, a.kc);
-  auto kern = k_gt_tc<MODE>;
+template <int MODE, uint32_t BN>
+cudaError_t launch_bn(const CUtensorMap& ta, const CUtensorMap& tb, const Args& a, int num_sms,
+                      cudaStream_t st) {
+  const size_t smem = smem_bytes<BN>(a.kc, a.stages);
+  auto kern = k_gt_tc<MODE, BN>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
   if (e != cudaSuccess) return e;
-  const uint32_t q_tiles = (a.nq + kRows * a.mt - 1) / (kRows * a.mt);
+  constexpr uint32_t rows_per_tile = kRows * (256 / BN);
+  const uint32_t q_tiles = (a.nq + rows_per_tile - 1) / rows_per_tile;
   const uint32_t grid = q_tiles < static_cast<uint32_t>(num_sms) ? q_tiles
                                                                   : static_cast<uint32_t>(num_sms);
   kern<<<grid ? grid : 1, kThreads, smem, st>>>(ta, tb, a);
   return cudaGetLastError();
+}
+
+// The launched shape: 256 base rows per tile against one 128-row query tile (measured faster
+// than 128 base rows against two query tiles: 1.12 s against 1.28 s for 1M x 1M x 200).
+constexpr uint32_t kBN = 256;
+
+template <int MODE>
+cudaError_t launch(const CUtensorMap& ta, const CUtensorMap& tb, const Args& a, int num_sms,
+                   cudaStream_t st) {
+  return launch_bn<MODE, kBN>(ta, tb, a, num_sms, st);
 }
 
 }  // namespace tc
@@ -774,7 +871,11 @@ int blocks_for(uint64_t warps, int per_block, int num_sms, int per_sm) {
   return static_cast<int>(b ? b : 1);
 }
 
-uint32_t padded_dim(uint32_t d) { return (d + tc::kChunk - 1) / tc::kChunk * tc::kChunk; }
+// FP16 rows are zero-padded to a multiple of 16 elements (one MMA K step); TMA reads the last
+// 64-element box past the row end as zeros.
+uint32_t padded_dim(uint32_t d) { return (d + 15) / 16 * 16; }
+uint32_t k_boxes(uint32_t dp) { return (dp + tc::kChunk - 1) / tc::kChunk; }
+uint32_t k_last(uint32_t dp) { return (dp - (k_boxes(dp) - 1) * tc::kChunk) / 16; }
 
 }  // namespace
 
@@ -785,18 +886,31 @@ uint32_t gt_max_dim() { return tc::kChunk * tc::kMaxKc; }
 GtPlan gt_plan(uint64_t n, uint64_t nq, uint32_t d, int num_sms, size_t smem_optin) {
   GtPlan p{};
   p.dp = padded_dim(d);
-  p.kc = p.dp / tc::kChunk;
-  p.mt = tc::pick_mt(p.kc, smem_optin);
-  // groups of gs rows, as many as keep G >= 8192 groups (or one row per group for small n)
-  p.gs = 1;
-  while (p.gs < 4096 && n / (2ull * p.gs) >= 8192) p.gs *= 2;
-  p.groups = static_cast<uint32_t>((n + p.gs - 1) / p.gs);
+  p.kc = k_boxes(p.dp);
+  p.bn = tc::kBN;
+  p.stages = tc::stages_for<tc::kBN>(p.kc, smem_optin);
+  // groups of base rows for the threshold pass, about 4096 or more per query where n allows:
+  // each epilogue thread's chunks (32 columns of one half of each tile), `span` at a time, or
+  // for small n groups of gs < 32 columns
+  const uint64_t n_tiles = (n + p.bn - 1) / p.bn;
+  const uint64_t chunks = n_tiles * (p.bn / 64);  // per thread
+  if (2 * chunks >= 4096) {
+    p.span = 1;
+    while (2 * ((chunks + 2 * p.span - 1) / (2 * p.span)) >= 4096) p.span *= 2;
+    p.gs = 0;
+    p.groups = static_cast<uint32_t>(2 * ((chunks + p.span - 1) / p.span));
+  } else {
+    p.span = 0;
+    p.gs = 1;
+    while (p.gs < 16 && n / (2ull * p.gs) >= 4096) p.gs *= 2;
+    p.groups = static_cast<uint32_t>((n + p.gs - 1) / p.gs);
+  }
   // queries per chunk: whole waves of query tiles, the chunk's maxima and candidate lists
   // within 4 GB
-  const uint64_t wave = static_cast<uint64_t>(tc::kRows) * p.mt * static_cast<uint64_t>(num_sms);
+  const uint64_t wave = 256ull * static_cast<uint64_t>(num_sms);
   const uint64_t per_q = static_cast<uint64_t>(p.groups) * 4 + kGtCap * 8 + 16;
   uint64_t cq = (4ull << 30) / per_q / wave * wave;
-  if (cq < static_cast<uint64_t>(tc::kRows) * p.mt) cq = static_cast<uint64_t>(tc::kRows) * p.mt;
+  if (cq < 256) cq = 256;
   if (cq > nq) cq = nq;
   p.cq = cq;
   return p;
@@ -805,7 +919,7 @@ GtPlan gt_plan(uint64_t n, uint64_t nq, uint32_t d, int num_sms, size_t smem_opt
 size_t gt_workspace_bytes(const GtPlan& p, uint64_t n, uint64_t nq) {
   auto al = [](uint64_t b) { return (b + 1023) & ~1023ull; };
   return al(n * p.dp * 2) + al(nq * p.dp * 2) + 2 * al(n * 4) + 2 * al(nq * 4) + al(8) +
-         2 * al(p.cq * 4) + al(p.cq * p.groups * 4) + al(p.cq * kGtCap * 8) + al(p.cq * 4);
+         2 * al(p.cq * 4) + al(p.cq * p.groups * 4) + al(p.cq * kGtCap * 8) + al(p.cq * 8);
 }
 
 int ground_truth(const GtPlan& plan, const float* base, uint64_t n, uint32_t d,
@@ -831,7 +945,7 @@ int ground_truth(const GtPlan& plan, const float* base, uint64_t n, uint32_t d,
   float* lo = reinterpret_cast<float*>(take(cq * 4));
   float* maxima = reinterpret_cast<float*>(take(cq * plan.groups * 4));
   uint64_t* cand = reinterpret_cast<uint64_t*>(take(cq * kGtCap * 8));
-  uint32_t* cand_cnt = reinterpret_cast<uint32_t*>(take(cq * 4));
+  uint32_t* cand_cnt = reinterpret_cast<uint32_t*>(take(cq * 8));
 
   cudaError_t e;
   k_half_rows<<<blocks_for(n, 8, num_sms, 8), 256, 0, st>>>(base, n, d, dp, b16, bn, be, status);
@@ -854,7 +968,9 @@ int ground_truth(const GtPlan& plan, const float* base, uint64_t n, uint32_t d,
     a.nq = rows;
     a.n = static_cast<uint32_t>(n);
     a.kc = plan.kc;
-    a.mt = plan.mt;
+    a.klast = k_last(dp);
+    a.stages = plan.stages;
+    a.span = plan.span;
     a.gs = plan.gs;
     a.groups = plan.groups;
     a.maxima = maxima;
@@ -924,9 +1040,10 @@ int screen_scores(const float* a, uint64_t na, const float* b, uint64_t nb, uint
   x.q0 = 0;
   x.nq = static_cast<uint32_t>(na);
   x.n = static_cast<uint32_t>(nb);
-  x.kc = dp / tc::kChunk;
-  x.mt = tc::pick_mt(x.kc, smem_optin);
-  x.gs = 1;
+  x.kc = k_boxes(dp);
+  x.klast = k_last(dp);
+  x.stages = tc::stages_for<tc::kBN>(x.kc, smem_optin);
+  x.span = 1;
   x.groups = 1;
   x.dump = out;
   x.status = status;

@@ -144,11 +144,13 @@ cudaError_t launch_fusion_final(const FusionArgs& a, int num_sms, cudaStream_t s
 // device-side problems set bits in *status (1 << 4: a value beyond the FP16 range, 1 << 6: a
 // query with more candidates than the selection holds, kErrWait: a bounded wait gave up).
 struct GtPlan {
-  uint32_t dp;      // d rounded up to a multiple of 64 (FP16 rows zero-padded)
-  uint32_t kc;      // dp / 64
-  uint32_t mt;      // 128-row M tiles per CTA (1 or 2)
-  uint32_t gs;      // base rows per group of the threshold pass
-  uint32_t groups;  // ceil(n / gs)
+  uint32_t dp;      // d rounded up to a multiple of 16 (FP16 rows zero-padded)
+  uint32_t kc;      // 64-element K boxes per row: ceil(dp / 64)
+  uint32_t bn;      // base rows per tile (256, against one 128-row query tile)
+  uint32_t stages;  // B ring stages
+  uint32_t span;    // threshold pass: chunks of 32 columns per group (0: groups of gs columns)
+  uint32_t gs;      // threshold pass, small n: columns per group
+  uint32_t groups;  // groups per query
   uint64_t cq;      // queries per chunk
 };
 uint32_t gt_max_k();

@@ -2,7 +2,8 @@
 inner products, ties to the lower id) checked against numpy on the CPU, and the GPU's FP16
 tensor-core screening (a tcgen05 GEMM with a selecting epilogue) + FP64 re-scoring checked
 against the oracle id for id -- over sizes that leave partial 128-row tiles, group sizes of the
-threshold pass from 1 to 8 rows, padded dimensions 36 -> 64 and 512 -- and the screening product
+threshold pass from 1 to 16 rows, dimensions that end inside a 64-element TMA box (36, 200) --
+and the screening product
 alone checked against exact products within its FP32 accumulation bound."""
 import numpy as np
 import pytest
@@ -69,7 +70,7 @@ def test_gpu_screen_scores_within_fp32_accumulation_bound(na, nb, d):
     """pg_screen_scores (the tcgen05 screening GEMM of pg_ground_truth, FP16 operands, FP32
     accumulation in TMEM) against the exact FP64 products of the same FP16-rounded operands:
     every score within the accumulation bound (d' * 2^-22) * sum |a_i b_i|, d' = d padded to a
-    multiple of 64, plus 16."""
+    multiple of 16, plus 16."""
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -84,7 +85,7 @@ def test_gpu_screen_scores_within_fp32_accumulation_bound(na, nb, d):
     ah, bh = a.half().double(), b.half().double()
     exact = ah @ bh.T
     mag = ah.abs() @ bh.abs().T
-    dp = (d + 63) // 64 * 64
+    dp = (d + 15) // 16 * 16
     bound = (dp + 16) * 2.0 ** -22 * mag + 1e-30
     err = (out.double() - exact).abs()
     assert torch.isfinite(out).all()
