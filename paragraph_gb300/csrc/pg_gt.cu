@@ -753,14 +753,19 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (uint32_t j = 0; j < 32; j++)
               hit |= (__uint_as_float(v[i][j]) >= lo[m]) ? (1u << j) : 0u;
             hit &= inr;
-            if (hit) {
-              uint64_t* dst = a.cand + static_cast<uint64_t>(qrow[m]) * kGtCap + half * kHalfCap;
+            if (hit) {  // rare (about 1.1 k hits per row): a short loop over a local copy, so the
+                        // unrolled common path stays small in the instruction cache
+              float tmp[32];
 #pragma unroll
-              for (uint32_t j = 0; j < 32; j++)
-                if ((hit >> j) & 1u) {
-                  if (cnt[m] < kHalfCap) dst[cnt[m]] = desc_key(__uint_as_float(v[i][j]), col0 + j);
-                  cnt[m]++;
-                }
+              for (uint32_t j = 0; j < 32; j++) tmp[j] = __uint_as_float(v[i][j]);
+              uint64_t* dst = a.cand + static_cast<uint64_t>(qrow[m]) * kGtCap + half * kHalfCap;
+#pragma unroll 1
+              while (hit) {
+                const uint32_t j = static_cast<uint32_t>(__ffs(static_cast<int>(hit)) - 1);
+                hit &= hit - 1u;
+                if (cnt[m] < kHalfCap) dst[cnt[m]] = desc_key(tmp[j], col0 + j);
+                cnt[m]++;
+              }
             }
           } else {
             float* o = a.dump + static_cast<uint64_t>(qrow[m]) * a.n;
