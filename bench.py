@@ -80,8 +80,8 @@ def parse():
     ap.add_argument("--no-gt", action="store_true",
                     help="skip timing the exact ground-truth generation (pg_ground_truth)")
     ap.add_argument("--no-secondary", action="store_true",
-                    help="skip the 1M x 512 cosine (M=48, L=96) configuration timed beside the "
-                         "headline")
+                    help="skip the 1M x 512 cosine (M=48, L=96) and the batched (64 sub-indexes, "
+                         "D=512) configurations timed beside the headline")
     ap.add_argument("--autotune", action="store_true",
                     help="run pg_autotune (launch shapes only; results unchanged) before timing")
     return ap.parse_args()
@@ -176,11 +176,35 @@ def allmax(x, world):
     return float(t.item())
 
 
+# Above this many points the data generator's float32 top-k would scan a score matrix of
+# terabytes; the workload's exact top-128 then comes from pg_ground_truth.
+GT_ON_GPU_ABOVE = 2_000_000
+
+
 def gpu_workload(args, device, queries: bool = False):
+    """(base, gt[, queries]) on the device, and the ms pg_ground_truth took (None when the data
+    generator's float32 top-k made the ground truth)."""
     from paragraph_gb300 import datagen
-    return datagen.make_dataset_cuda(args.n, args.d, gt_k=128, seed=args.seed, device=device,
-                                     return_queries=queries, cosine=args.cosine,
-                                     centers=args.centers)
+    if args.n <= GT_ON_GPU_ABOVE:
+        return datagen.make_dataset_cuda(args.n, args.d, gt_k=128, seed=args.seed, device=device,
+                                         return_queries=queries, cosine=args.cosine,
+                                         centers=args.centers), None
+    import torch
+    import paragraph_gb300 as pg
+    base, _, q = datagen.make_dataset_cuda(args.n, args.d, seed=args.seed, device=device,
+                                           cosine=args.cosine, centers=args.centers,
+                                           with_gt=False)
+    gt = torch.empty((args.n, 128), dtype=torch.int32, device=device)
+    stream = torch.cuda.Stream(device)
+    dev_index = torch.device(device).index or 0
+    with pg.Handle(dev_index, stream=stream) as h:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.ground_truth(base, q, gt)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    return ((base, gt, q) if queries else (base, gt)), e0.elapsed_time(e1)
 
 
 # DRAM bytes (read + write) per launch of the search kernel on the default workload
@@ -369,7 +393,7 @@ def run_reference(args):
 
     import oracle
     if torch.cuda.is_available():
-        base, gt = gpu_workload(args, "cuda")
+        (base, gt), _ = gpu_workload(args, "cuda")
         base_np = base.cpu().numpy()
         gt_np = gt.cpu().numpy().view(np.uint32)
         del base, gt
@@ -421,7 +445,7 @@ def run_ours(args):
     import paragraph_gb300 as pg
     dev = torch.device("cuda", local)
     want_q = not args.no_gt
-    wl = gpu_workload(args, dev, queries=want_q)
+    wl, gt_gen_ms = gpu_workload(args, dev, queries=want_q)
     base, gt = wl[0], wl[1]
     queries = wl[2] if want_q else None
     torch.cuda.synchronize()
@@ -507,9 +531,15 @@ def run_ours(args):
         del iout, icnt
     # the build's input, ground truth top-128, generated exactly on the GPU (pg_ground_truth)
     gt_line = None
+    if gt_gen_ms is not None:  # the workload's own ground truth came from pg_ground_truth
+        gt_line = {"ms": round(gt_gen_ms, 1), "queries": int(n), "base": int(n), "k": 128,
+                   "screen_gemm_tflops_equiv": round(2.0 * n * n * d / (gt_gen_ms / 1e3) / 1e12, 1),
+                   "definition": "exact FP64 inner products, ties to the lower id (this is the "
+                                 "build's input here: the float32 top-k is not run at this size)"}
+        queries = None
     if queries is not None:
         gout = torch.empty((queries.shape[0], 128), dtype=torch.int32, device=dev)
-        h.ground_truth(base, queries[:1024], gout[:1024])  # cuBLAS and workspace set-up
+        h.ground_truth(base, queries[:1024], gout[:1024])  # workspace set-up
         torch.cuda.synchronize()
         g0 = torch.cuda.Event(enable_timing=True)
         g1 = torch.cuda.Event(enable_timing=True)
@@ -527,9 +557,10 @@ def run_ours(args):
                                  "benchmark's own ground truth is a float32 top-k"}
         del gout, queries
         torch.cuda.empty_cache()
-    secondary = None
+    secondary = batched = None
     if not args.no_secondary and args.n == 1_000_000 and args.d == 200 and not args.cosine:
         secondary = secondary_cosine(args, h, dev, stream)
+        batched = batched_secondary(args, h, dev, stream)
     evals = stats[-1].evals_total
     assert all(s.evals_total == evals for s in stats), "evaluation count changed between builds"
     value = evals * args.steps * world / (ms_total / 1e3)
@@ -543,7 +574,7 @@ def run_ours(args):
         proj_h = torch.empty((n, 16), dtype=torch.int32).pin_memory()
         del base, gt
         torch.cuda.empty_cache()
-        for _ in range(1):
+        for _ in range(2):
             h.build_host_ptr(base_h.data_ptr(), n, d, gt_h.data_ptr(), gt_h.shape[0],
                              graph_h.data_ptr(), proj_h.data_ptr(), params)
         barrier(world)
@@ -609,6 +640,7 @@ def run_ours(args):
                 "index": index_line,
                 "ground_truth": gt_line,
                 "secondary": secondary,
+                "batched": batched,
                 "gpu_launches": launches_per_build * args.steps,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary()}
@@ -620,31 +652,25 @@ def run_ours(args):
     return 0
 
 
-def run_batched(args):
-    """Batched form: S independent sub-indexes of uneven (seeded log-uniform) sizes, each with its
-    own training queries (Q = N) and exact top-128 ground truth (pg_ground_truth), built in one
-    CUDA-graph-captured pass (pg_build_batched_device) against building them one by one."""
+def batched_workload(count, d, min_points, max_points, seed, cosine, centers, h, dev, stream):
+    """`count` sub-indexes of seeded log-uniform sizes, each with its own training queries (Q = N)
+    and exact top-128 ground truth from pg_ground_truth.  Returns (base, gt, node_off, sizes,
+    ground-truth ms, generation s)."""
     import numpy as np
     import torch
-    import paragraph_gb300 as pg
     from paragraph_gb300 import datagen
-    dev = torch.device("cuda", 0)
-    rng = np.random.Generator(np.random.PCG64(args.seed))
-    sizes = np.exp(rng.uniform(np.log(args.min_points), np.log(args.max_points),
-                               args.batched)).astype(np.int64)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sizes = np.exp(rng.uniform(np.log(min_points), np.log(max_points), count)).astype(np.int64)
     node_off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
     total = int(node_off[-1])
-    base = torch.empty((total, args.d), dtype=torch.float32, device=dev)
+    base = torch.empty((total, d), dtype=torch.float32, device=dev)
     gt = torch.empty((total, 128), dtype=torch.int32, device=dev)
-    stream = torch.cuda.Stream(dev)
-    h = pg.Handle(0, stream=stream)
     t0 = time.perf_counter()
     gt_ms = 0.0
     for i, ni in enumerate(sizes):
         lo, hi = int(node_off[i]), int(node_off[i + 1])
-        b, _, q = datagen.make_dataset_cuda(int(ni), args.d, seed=args.seed + 1 + i, device=dev,
-                                            cosine=args.cosine, centers=args.centers,
-                                            with_gt=False)
+        b, _, q = datagen.make_dataset_cuda(int(ni), d, seed=seed + 1 + i, device=dev,
+                                            cosine=cosine, centers=centers, with_gt=False)
         base[lo:hi] = b
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -656,42 +682,102 @@ def run_batched(args):
         gt_ms += e0.elapsed_time(e1)
         del b, q
     torch.cuda.empty_cache()
-    gen_s = time.perf_counter() - t0
-    screen = {"bf16": pg.SCREEN_BF16, "fp16": pg.SCREEN_FP16, "none": pg.SCREEN_NONE}[args.screen]
-    params = pg.default_params(args.degree, args.beam, screen=screen, flags=pg.FLAG_CUDA_GRAPH)
-    tuning = None
-    if args.autotune:
-        _, tun = h.autotune(base, gt, params, node_off=node_off, query_off=node_off)
-        tuning = tun.as_dict()
-    graph = torch.empty((total, args.degree), dtype=torch.int32, device=dev)
-    for _ in range(args.warmup):
+    return base, gt, node_off, sizes, gt_ms, time.perf_counter() - t0
+
+
+def batched_measure(h, stream, base, gt, node_off, sizes, degree, beam, screen, steps, warmup):
+    """One CUDA-graph replay of pg_build_batched_device over every sub-index against building
+    them one by one (same screen; and the plain FP32 path for the identical-edges check).
+    Returns (dict, Stats of the last batched build, ms per batched build)."""
+    import torch
+    import paragraph_gb300 as pg
+    params = pg.default_params(degree, beam, screen=screen, flags=pg.FLAG_CUDA_GRAPH)
+    total = int(node_off[-1])
+    graph = torch.empty((total, degree), dtype=torch.int32, device=base.device)
+    for _ in range(warmup):
         st = h.build_batched(base, gt, node_off, node_off, graph, None, params)
     torch.cuda.synchronize()
-    with ClockSampler(0) as clocks:
-        a = torch.cuda.Event(enable_timing=True)
-        b_ = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        for _ in range(args.steps):
-            st = h.build_batched(base, gt, node_off, node_off, graph, None, params)
-        b_.record(stream)
-        torch.cuda.synchronize()
-    ms = a.elapsed_time(b_) / args.steps
-    # one by one, same parameters, no graph
-    p1 = pg.default_params(args.degree, args.beam, screen=screen)
-    alone = torch.empty_like(graph)
-    for i, ni in enumerate(sizes):  # warm-up
-        lo, hi = int(node_off[i]), int(node_off[i + 1])
-        h.build_device(base[lo:hi], gt[lo:hi], alone[lo:hi], None, p1)
-    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b_ = torch.cuda.Event(enable_timing=True)
     a.record(stream)
-    ev_alone = 0
-    for i, ni in enumerate(sizes):
-        lo, hi = int(node_off[i]), int(node_off[i + 1])
-        ev_alone += h.build_device(base[lo:hi], gt[lo:hi], alone[lo:hi], None, p1).evals_total
+    for _ in range(steps):
+        st = h.build_batched(base, gt, node_off, node_off, graph, None, params)
     b_.record(stream)
     torch.cuda.synchronize()
-    ms_alone = a.elapsed_time(b_)
-    identical = bool(torch.equal(graph, alone))
+    ms = a.elapsed_time(b_) / steps
+
+    def one_by_one(p):
+        out = torch.empty_like(graph)
+        for i in range(len(sizes)):  # warm-up pass
+            lo, hi = int(node_off[i]), int(node_off[i + 1])
+            h.build_device(base[lo:hi], gt[lo:hi], out[lo:hi], None, p)
+        torch.cuda.synchronize()
+        a.record(stream)
+        ev = 0
+        for i in range(len(sizes)):
+            lo, hi = int(node_off[i]), int(node_off[i + 1])
+            ev += h.build_device(base[lo:hi], gt[lo:hi], out[lo:hi], None, p).evals_total
+        b_.record(stream)
+        torch.cuda.synchronize()
+        return out, ev, a.elapsed_time(b_)
+
+    alone, ev_alone, ms_alone = one_by_one(pg.default_params(degree, beam, screen=screen))
+    out = {"ms_batched": round(ms, 3), "evals": int(st.evals_total),
+           "evals_per_s": st.evals_total / (ms / 1e3),
+           "one_by_one": {"ms": round(ms_alone, 3), "evals": int(ev_alone),
+                          "identical_edges": bool(torch.equal(graph, alone)),
+                          "speedup_of_batched": round(ms_alone / ms, 3)}}
+    del alone
+    if screen:
+        plain, _, ms_plain = one_by_one(pg.default_params(degree, beam, screen=pg.SCREEN_NONE))
+        out["plain_one_by_one"] = {"ms": round(ms_plain, 3),
+                                   "identical_edges": bool(torch.equal(graph, plain))}
+        del plain
+    return out, st, ms
+
+
+def batched_secondary(args, h, dev, stream):
+    """The batched configuration, measured beside the headline: 64 sub-indexes of log-uniform
+    sizes in [10k, 500k], D = 512, inner product, M = 32, L = 64."""
+    import torch
+    count, d = 64, 512
+    base, gt, node_off, sizes, gt_ms, gen_s = batched_workload(
+        count, d, 10_000, 500_000, args.seed, False, args.centers, h, dev, stream)
+    screen = {"bf16": 1, "fp16": 3, "none": 0}[args.screen]
+    res, _, _ = batched_measure(h, stream, base, gt, node_off, sizes, 32, 64, screen, 2, 1)
+    res.update({"workload": f"{count} sub-indexes, sizes log-uniform in [10000, 500000] "
+                            f"(total {int(node_off[-1])}), D={d}, IP, M=32, L=64, one "
+                            "CUDA-graph replay",
+                "sizes_min_max": [int(sizes.min()), int(sizes.max())],
+                "ground_truth_ms_total": round(gt_ms, 1), "data_generation_s": round(gen_s, 1)})
+    del base, gt
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_batched(args):
+    """Batched form: S independent sub-indexes of uneven (seeded log-uniform) sizes, each with its
+    own training queries (Q = N) and exact top-128 ground truth (pg_ground_truth), built in one
+    CUDA-graph-captured pass (pg_build_batched_device) against building them one by one."""
+    import torch
+    import paragraph_gb300 as pg
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    h = pg.Handle(0, stream=stream)
+    base, gt, node_off, sizes, gt_ms, gen_s = batched_workload(
+        args.batched, args.d, args.min_points, args.max_points, args.seed, args.cosine,
+        args.centers, h, dev, stream)
+    total = int(node_off[-1])
+    screen = {"bf16": pg.SCREEN_BF16, "fp16": pg.SCREEN_FP16, "none": pg.SCREEN_NONE}[args.screen]
+    tuning = None
+    if args.autotune:
+        params = pg.default_params(args.degree, args.beam, screen=screen, flags=pg.FLAG_CUDA_GRAPH)
+        _, tun = h.autotune(base, gt, params, node_off=node_off, query_off=node_off)
+        tuning = tun.as_dict()
+    with ClockSampler(0) as clocks:
+        res, st, ms = batched_measure(h, stream, base, gt, node_off, sizes, args.degree,
+                                      args.beam, screen, args.steps, args.warmup)
+    launches = (10 + 8 * 2 + 1 + (1 if screen and args.beam <= 96 else 0)) * args.steps
     line = {"metric": metric_name(args, total), "value": st.evals_total / (ms / 1e3),
             "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
@@ -702,16 +788,11 @@ def run_batched(args):
                                    f"D={args.d}, {'cosine' if args.cosine else 'IP'}, "
                                    f"M={args.degree}, L={args.beam}, one CUDA-graph replay",
                        "sizes_min_max": [int(sizes.min()), int(sizes.max())], "total": total},
-            "one_by_one": {"ms": round(ms_alone, 3), "evals": int(ev_alone),
-                           "identical_edges": identical,
-                           "speedup_of_batched": round(ms_alone / ms, 3)},
+            "one_by_one": res["one_by_one"], "plain_one_by_one": res.get("plain_one_by_one"),
             "ground_truth": {"ms_total": round(gt_ms, 1), "k": 128,
                              "definition": "exact FP64 inner products (pg_ground_truth)"},
             "data_generation_s": round(gen_s, 1), "tuning": tuning,
-            "gpu_launches": (10 + 8 * params.link_rounds
-                             + (1 if params.link_rounds > 0 else 0)
-                             + (1 if screen and params.link_rounds > 0 and args.beam <= 96 else 0))
-                            * args.steps, "clocks": clocks.summary()}
+            "gpu_launches": launches, "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
     h.close()
     return 0
