@@ -207,10 +207,13 @@ def gpu_workload(args, device, queries: bool = False):
     return ((base, gt, q) if queries else (base, gt)), e0.elapsed_time(e1)
 
 
-# DRAM bytes (read + write) per launch of the search kernel on the default workload
-# (1M x 200 IP, M = 32, L = 64, FP16-screened build), measured by ncu
-# (profiles/k_search_m32_1Mx200_dram.md): round 1 over the projection, round 2 over the link graph.
-SEARCH_DRAM_BYTES = {(1_000_000, 200, 32, 64, False): None}
+# DRAM bytes (read + write) per launch of the search kernel, measured by ncu on these workloads
+# (profiles/search_dram_1Mx200_1Mx512cos.md): round 1 over the projection, round 2 over the link
+# graph.  Keys: (n, d, M, L, cosine).
+SEARCH_DRAM_BYTES = {
+    (1_000_000, 200, 32, 64, False): (1_217_476_352, 1_182_223_104),
+    (1_000_000, 512, 48, 96, True): (143_634_611_456, 870_972_185_088),
+}
 
 
 def search_roofline(st, args, peak_gbs, peak_kind, rounds):
@@ -236,8 +239,11 @@ def search_roofline(st, args, peak_gbs, peak_kind, rounds):
     dram = SEARCH_DRAM_BYTES.get((args.n, args.d, args.degree, args.beam, bool(args.cosine)))
     traffic = dram[last] if dram else None
     kname = "k_search_m32" if args.beam - 32 <= 32 else "k_search_mk"
+    dram_frac = traffic / (ms / 1e3) / 1e9 / peak_gbs if traffic else None
+    bound = ("hbm: DRAM-served row gathers (see dram_frac)" if dram_frac and dram_frac >= 0.4
+             else "latency: L2-resident row gathers, not HBM (see dram_frac)")
     out = {"kernel": f"{kname} (round-{last + 1} beam search)",
-           "bound": "latency: L2-resident row gathers, not HBM (see dram_frac)",
+           "bound": bound,
            "achieved": round(achieved, 1), "peak": peak_gbs, "peak_kind": peak_kind,
            "unit": "GB/s", "frac": round(achieved / peak_gbs, 4),
            "frac_meaning": "algorithmic gathered bytes / launch time / measured HBM copy peak",
@@ -313,6 +319,8 @@ def secondary_cosine(args, h, dev, stream):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / k
         graphs[name] = (graph, proj)
+        if screen:
+            st_fp16 = st
         out[name] = {"ms_per_build": round(ms, 2), "evals": int(st.evals_total),
                      "evals_per_s": st.evals_total / (ms / 1e3),
                      "stage_ms": {"proj": round(st.ms_proj, 2),
@@ -329,8 +337,10 @@ def secondary_cosine(args, h, dev, stream):
     worst, npairs = screen_error_sample(base, graphs["plain"][0])
     out["fp16_max_rel_error_vs_fp64"] = worst
     out["error_sample"] = f"{npairs} random graph edges, |s16 - s64| / (|x||y|)"
-    dram = SEARCH_DRAM_BYTES.get((n, d, m, beam, True))
-    out["search_dram_bytes_per_launch"] = list(dram) if dram else None
+    # the round-2 search of this build against the HBM roofline (it is the DRAM-heavy search:
+    # 1M rows of 2 KB, about 43% of the gathers served by L2)
+    shape = argparse.Namespace(n=n, d=d, degree=m, beam=beam, cosine=True)
+    out["search_roofline"] = search_roofline(st_fp16, shape, *peaks(), 2)
     del base, gt, graphs
     torch.cuda.empty_cache()
     return out
