@@ -108,7 +108,7 @@ typedef struct pg_tuning {
   uint32_t search_rows;         /* candidate rows staged per pass in the Km=32 search: 8 or 16 */
   uint32_t search_warps_per_sm; /* cap on resident search warps per SM (0 = occupancy maximum) */
   uint32_t hash_factor;         /* visited-set capacity multiplier over the exact minimum: 1, 2, 4 */
-  uint32_t screen_carveout;     /* shared-memory carveout (%) of the screened prune (0 = 76) */
+  uint32_t screen_stages;       /* row-copy ring depth of the screened prune: 0 (= 2), 2, 3, 4 */
   uint32_t beam;                /* L chosen by pg_autotune's recall target (0 = not tuned) */
   float recall;                 /* recall@10 measured for `beam` (when tuned) */
   float ms_build;               /* build time measured with this tuning */
@@ -217,7 +217,7 @@ int pg_screen_scores(pg_handle h, const float* d_a, uint64_t na, const float* d_
  * capacity are compile-time constants, tests/test_t2iend.cu:671-727) --------------------------
  * pg_set_tuning / pg_get_tuning: the tuning later builds on this handle use.
  * pg_autotune: times trial builds of the given data and keeps the fastest choice of search
- * staging rows, resident search warps, visited-set capacity and screened-prune carveout
+ * staging rows, resident search warps, visited-set capacity and screened-prune copy-ring depth
  * (coordinate search from the defaults, each candidate timed twice, kept only when it wins by
  * more than 1%).  When d_queries (the training queries behind d_gt, q_i x d per sub-index) and
  * target_recall > 0 are given, it first picks the beam: the smallest L in {64, 96, 128} whose

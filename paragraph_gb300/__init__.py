@@ -74,7 +74,7 @@ class Stats(ctypes.Structure):
 class Tuning(ctypes.Structure):
     """pg_tuning: launch shapes of a handle (results do not depend on them)."""
     _fields_ = [("search_rows", ctypes.c_uint32), ("search_warps_per_sm", ctypes.c_uint32),
-                ("hash_factor", ctypes.c_uint32), ("screen_carveout", ctypes.c_uint32),
+                ("hash_factor", ctypes.c_uint32), ("screen_stages", ctypes.c_uint32),
                 ("beam", ctypes.c_uint32), ("recall", ctypes.c_float),
                 ("ms_build", ctypes.c_float), ("ms_default", ctypes.c_float),
                 ("reserved", ctypes.c_uint32 * 8)]

@@ -17,9 +17,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libparagraph_gb300.so")
-SOURCES = ["pg_api.cu", "pg_graph.cu", "pg_search.cu", "pg_screen.cu", "pg_noalloc.cu",
-           "pg_roar.cu", "pg_gt.cu"]
-HEADERS = ["pg_device.cuh", "pg_kernels.h"]
+SOURCES = ["pg_api.cu", "pg_graph.cu", "pg_search.cu", "pg_screen.cu", "pg_prune_tc.cu",
+           "pg_noalloc.cu", "pg_roar.cu", "pg_gt.cu"]
+HEADERS = ["pg_device.cuh", "pg_kernels.h", "pg_tc.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "--expt-relaxed-constexpr"]

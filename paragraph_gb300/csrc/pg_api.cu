@@ -413,7 +413,7 @@ int run_build(pg_handle h, const pg_params* p, const float* base, uint64_t n, ui
       pr.evals = cnt + C_PRUNE + r;
       pr.status = h->d_status;
       pr.rescored = cnt + C_RESCORED + r;
-      pr.carveout = h->tune.screen_carveout;
+      pr.stages = h->tune.screen_stages;
       pr.screen_half = p->screen == PG_SCREEN_FP16;
       pr.norms = norms;
       if (screened) {
@@ -1077,7 +1077,8 @@ int pg_set_tuning(pg_handle h, const pg_tuning* t) {
   if (t->search_warps_per_sm > 64) return fail(PG_EINVAL, "search_warps_per_sm must be <= 64");
   if (t->hash_factor > 4 || t->hash_factor == 3)
     return fail(PG_EINVAL, "hash_factor=%u must be 0, 1, 2 or 4", t->hash_factor);
-  if (t->screen_carveout > 100) return fail(PG_EINVAL, "screen_carveout must be <= 100");
+  if (t->screen_stages == 1 || t->screen_stages > 4)
+    return fail(PG_EINVAL, "screen_stages must be 0, 2, 3 or 4");
   std::lock_guard<std::mutex> lk(h->mu);
   h->tune = *t;
   if (h->gexec) {  // a captured build holds the old launch shapes
@@ -1140,7 +1141,7 @@ int pg_autotune(pg_handle h, pg_params* p, const float* d_base, uint32_t d, cons
   pg_tuning best{};
   best.search_rows = 8;
   best.hash_factor = 1;
-  best.screen_carveout = 76;
+  best.screen_stages = 2;
   h->tune = best;
   pg_stats st;
 
@@ -1256,8 +1257,8 @@ int pg_autotune(pg_handle h, pg_params* p, const float* d_base, uint32_t d, cons
       if (rc) return restore(rc);
     }
     if (tp.screen != PG_SCREEN_NONE) {
-      for (uint32_t c : {50u, 100u, 25u}) {
-        rc = try_value(&pg_tuning::screen_carveout, c);
+      for (uint32_t c : {3u, 4u}) {
+        rc = try_value(&pg_tuning::screen_stages, c);
         if (rc) return restore(rc);
       }
     }

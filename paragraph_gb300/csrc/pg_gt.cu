@@ -31,6 +31,7 @@
 
 #include "pg_device.cuh"
 #include "pg_kernels.h"
+#include "pg_tc.cuh"
 
 namespace pg {
 
@@ -376,6 +377,8 @@ __global__ void __launch_bounds__(256) k_gt_theta(const float* __restrict__ maxi
 // issued MMAs are drained and the TMEM is freed before the CTA exits.
 namespace tc {
 
+using namespace tcu;
+
 constexpr uint32_t kRows = 128;  // rows of an A tile (queries) and of a TMA box
 constexpr uint32_t kChunk = 64;  // K elements per TMA box
 constexpr uint32_t kBox = kRows * kChunk * 2;  // 16 KB
@@ -413,101 +416,9 @@ struct Args {
   uint32_t* status;
 };
 
-__device__ __forceinline__ uint32_t saddr(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ uint64_t now_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ void bar_init(uint64_t* b, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void bar_expect_tx(uint64_t* b, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bar_arrive(uint64_t* b) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(b)) : "memory");
-}
-__device__ __forceinline__ bool bar_try(uint64_t* b, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(saddr(b)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Waits for the phase of parity `parity` of *b; false after one second or when another role
-// has given up (*stop set).
-__device__ __forceinline__ bool bar_wait(uint64_t* b, uint32_t parity,
-                                         const volatile uint32_t* stop) {
-  if (bar_try(b, parity)) return true;
-  const uint64_t t0 = now_ns();
-  for (uint32_t i = 1;; i++) {
-    if (bar_try(b, parity)) return true;
-    if ((i & 31u) == 0) {
-      if (stop && *stop) return false;
-      if (now_ns() - t0 > 1000000000ull) return false;
-    }
-  }
-}
-__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, uint32_t x,
-                                         uint32_t y, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(saddr(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(saddr(bar))
-      : "memory");
-}
-// Shared-memory descriptor of a K-major tile written by TMA with 128-byte swizzling: rows of
-// 128 bytes in 8-row atoms of 1024 bytes (stride byte offset), one atom along K (leading byte
-// offset unused), descriptor version 1 (bits 46-47), swizzle mode 2 (bits 61-63).  The start
-// address steps 32 bytes per K = 16 slice inside the atom.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
-  return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) | (static_cast<uint64_t>(1024 >> 4) << 32) |
-         (1ull << 46) | (2ull << 61);
-}
 template <uint32_t BN>
 __device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(idesc<BN>()), "r"(acc)
-      : "memory");
-}
-__device__ __forceinline__ void commit(uint64_t* bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          saddr(bar))
-      : "memory");
-}
-__device__ __forceinline__ void fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-// 32 consecutive FP32 columns of this thread's TMEM lane into v[0..31] (no wait).
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
-      "%28, %29, %30, %31}, [%32];"
-      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
-        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
-        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-      : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_wait_ld() {
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  mma_f16(d_tmem, a, b, idesc<BN>(), acc);
 }
 
 __device__ __forceinline__ float max32(const uint32_t* v) {  // pairwise tree, 31 FMNMX
@@ -798,26 +709,6 @@ __global__ void __launch_bounds__(kThreads, 1)
                  "r"(ncols)
                  : "memory");
   }
-}
-
-using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                 const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                 const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-// cuTensorMapEncodeTiled through the runtime's driver entry points (no link to the driver
-// library); looked up once per process.
-EncodeTiled encoder() {
-  static EncodeTiled fn = []() -> EncodeTiled {
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
-                                         &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      return nullptr;
-    return reinterpret_cast<EncodeTiled>(f);
-  }();
-  return fn;
 }
 
 // A rows x dp FP16 matrix (row stride dp * 2 bytes, a multiple of 32) as TMA boxes of

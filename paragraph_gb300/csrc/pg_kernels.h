@@ -28,9 +28,9 @@ struct PruneArgs {
   const uint64_t* seg_off;
   const uint64_t* qseg_off;
   uint32_t seg_count;
-  // screened kernel: preferred shared-memory carveout in percent (0 = 76); results do not
+  // screened kernel: depth of its row-copy ring (0 = default, else 2..4); results do not
   // depend on it
-  uint32_t carveout;
+  uint32_t stages;
   uint32_t screen_half;  // screened kernel: FP16 operands instead of BF16
   // screened kernel: per point (|x|, |x - x^| + |x^_sub|) upper bounds from launch_screen_norms
   // with the same screen_half
@@ -196,14 +196,15 @@ cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, c
 // Every query's 32 seed distances in the search's FP32 order into out (queries x 32).
 cudaError_t launch_seed_dists(const SearchArgs& a, float* out, int num_sms, cudaStream_t st);
 bool search_supported(uint32_t d, uint32_t km, uint32_t kp, uint32_t kd);
-// Screened (FP16 or BF16 tensor-core Gram + exact re-scoring) prune for strict rounds,
-// c <= 96, 4 <= d <= 1024, d % 4 == 0.
+// Screened prune for strict rounds (pg_prune_tc.cu): FP16 or BF16 candidate Gram on the tcgen05
+// tensor cores + exact re-scoring, 1 <= c <= 128, 4 <= d <= 1024, d % 4 == 0; the launch also
+// wants a 16-byte aligned base.
 bool screen_supported(uint32_t c, uint32_t d, int strict);
+cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_optin,
+                                cudaStream_t st);
 // Per-point norm bounds for the screened prune (FP16 rounding when half, else BF16): n float2.
 cudaError_t launch_screen_norms(const float* base, uint64_t n, uint32_t d, uint32_t half,
                                 float2* out, int num_sms, cudaStream_t st);
-cudaError_t launch_prune_screen(const PruneArgs& a, int num_sms, size_t smem_optin,
-                                cudaStream_t st);
 
 constexpr uint32_t kScanTileElems = 4096;
 

@@ -40,7 +40,7 @@ def _build(pg, h, base, gt, params):
 
 
 @pytest.mark.parametrize("field,value", [("search_rows", 16), ("search_warps_per_sm", 8),
-                                         ("hash_factor", 4), ("screen_carveout", 25)])
+                                         ("hash_factor", 4), ("screen_stages", 4)])
 def test_every_launch_shape_builds_the_same_graph(pg, data, field, value):
     base, _, gt = data
     db, dg = _dev(base), _dev(gt)
@@ -56,7 +56,7 @@ def test_every_launch_shape_builds_the_same_graph(pg, data, field, value):
 
 def test_bad_tuning_is_rejected(pg):
     with pg.Handle(0) as h:
-        for field, value in [("search_rows", 12), ("hash_factor", 3), ("screen_carveout", 101)]:
+        for field, value in [("search_rows", 12), ("hash_factor", 3), ("screen_stages", 5)]:
             t = pg.Tuning()
             setattr(t, field, value)
             with pytest.raises(pg.PGError) as e:

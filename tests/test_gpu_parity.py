@@ -313,14 +313,17 @@ def test_screened_build_with_hubs_and_duplicates(pg, handle, golden_dir, screen)
 
 
 @pytest.mark.parametrize("screen", [1, 3])  # BF16, FP16
-@pytest.mark.parametrize("n,d,degree,seed,cosine", [(8000, 512, 48, 5, True),
-                                                    (6000, 200, 32, 6, False)])
-def test_screened_build_96_candidates(pg, handle, n, d, degree, seed, cosine, screen):
-    """L = 96: the screened prune's three-slot variant (96 candidates, Gram in two passes)."""
+@pytest.mark.parametrize("n,d,degree,seed,cosine,beam", [(8000, 512, 48, 5, True, 96),
+                                                         (6000, 200, 32, 6, False, 96),
+                                                         (5000, 200, 32, 7, False, 128),
+                                                         (4000, 36, 24, 8, True, 128)])
+def test_screened_build_wide_beams(pg, handle, n, d, degree, seed, cosine, beam, screen):
+    """L = 96 and 128: the screened prune's one-node tiles (more than 64 candidates per node
+    fill a 128-row tensor-core tile on their own); D = 36 ends in a chunk of 4 columns."""
     from paragraph_gb300 import datagen
     base, q = datagen.make_base_queries(n, d, seed=seed, cosine=cosine)
     gt = datagen.ground_truth(base, q, 128)
-    g, p, st, ref = _build_both(pg, handle, base, gt, degree=degree, beam=96, screen=screen)
+    g, p, st, ref = _build_both(pg, handle, base, gt, degree=degree, beam=beam, screen=screen)
     assert np.array_equal(p, ref["proj"])
     bad = (g != ref["graph"]).any(axis=1)
     assert not bad.any(), f"{bad.sum()} rows differ"
