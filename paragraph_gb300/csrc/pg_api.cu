@@ -244,6 +244,22 @@ int check_params(const pg_params* p, uint64_t n, uint32_t d, uint64_t q) {
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
+// The device address of host memory p (bytes long) when it is pinned memory that the device can
+// address and the copy kernel can move (16-byte aligned, a multiple of 16 bytes); else nullptr.
+// cudaHostGetDevicePointer fails, without a sticky error, for memory that CUDA did not pin.
+const void* mapped_host(const void* p, size_t bytes) {
+  if (!p || !aligned16(p) || (bytes % 16) != 0) return nullptr;
+  void* dptr = nullptr;
+  if (cudaHostGetDevicePointer(&dptr, const_cast<void*>(p), 0) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return aligned16(dptr) ? dptr : nullptr;
+}
+void* mapped_host(void* p, size_t bytes) {
+  return const_cast<void*>(mapped_host(static_cast<const void*>(p), bytes));
+}
+
 int status_to_error(uint32_t s) {
   if (s & 4u) return fail(PG_EINVAL, "input holds an id >= n that is not tomb (status 0x%x)", s);
   if (s & 1u) return fail(PG_ETIMEOUT, "a search exceeded max_search_iters (status 0x%x)", s);
@@ -836,32 +852,46 @@ int pg_build_host(pg_handle h, const pg_params* p, const float* base, uint64_t n
     PG_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
     PG_CUDA(cudaEventCreateWithFlags(&h->copy_done, cudaEventDisableTiming));
   }
-  // the inputs' bytes split in two halves, one per stream, so that two copy engines share them
-  // (one copy reaches about 210 GB/s from pinned memory on GB300)
   const size_t hb = n * d * 4, hg = q * p->gt_k * 4;
-  const size_t b1 = std::min(hb, ((hb + hg) / 2) & ~static_cast<size_t>(4095));
   PG_CUDA(cudaEventRecord(t0, s));
-  PG_CUDA(cudaStreamWaitEvent(h->copy_stream, t0, 0));
-  PG_CUDA(cudaMemcpyAsync(d_base, base, b1, cudaMemcpyHostToDevice, s));
-  if (hb > b1)
-    PG_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(d_base) + b1,
-                            reinterpret_cast<const char*>(base) + b1, hb - b1,
-                            cudaMemcpyHostToDevice, h->copy_stream));
-  PG_CUDA(cudaMemcpyAsync(d_gt, gt, hg, cudaMemcpyHostToDevice, h->copy_stream));
-  PG_CUDA(cudaEventRecord(h->copy_done, h->copy_stream));
-  PG_CUDA(cudaStreamWaitEvent(s, h->copy_done, 0));
+  // Pinned host memory that the device can address (cudaHostGetDevicePointer succeeds) is read
+  // by a copy kernel: the SMs keep more requests in flight over the CPU-GPU link than the copy
+  // engines.  Other host memory goes through cudaMemcpyAsync, split over two streams so that two
+  // copy engines share it.
+  const void* mb = mapped_host(base, hb);
+  const void* mg = mapped_host(gt, hg);
+  if (mb && mg) {
+    PG_CUDA(pg::launch_copy16(d_base, mb, hb, h->num_sms, s));
+    PG_CUDA(pg::launch_copy16(d_gt, mg, hg, h->num_sms, s));
+  } else {
+    const size_t b1 = std::min(hb, ((hb + hg) / 2) & ~static_cast<size_t>(4095));
+    PG_CUDA(cudaStreamWaitEvent(h->copy_stream, t0, 0));
+    PG_CUDA(cudaMemcpyAsync(d_base, base, b1, cudaMemcpyHostToDevice, s));
+    if (hb > b1)
+      PG_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(d_base) + b1,
+                              reinterpret_cast<const char*>(base) + b1, hb - b1,
+                              cudaMemcpyHostToDevice, h->copy_stream));
+    PG_CUDA(cudaMemcpyAsync(d_gt, gt, hg, cudaMemcpyHostToDevice, h->copy_stream));
+    PG_CUDA(cudaEventRecord(h->copy_done, h->copy_stream));
+    PG_CUDA(cudaStreamWaitEvent(s, h->copy_done, 0));
+  }
   PG_CUDA(cudaEventRecord(t1, s));
   if (st) std::memset(st, 0, sizeof(*st));
   rc = run_build(h, p, d_base, n, d, d_gt, q, d_graph, d_proj, st);
   if (rc) return rc;
   PG_CUDA(cudaEventRecord(t2, s));
   uint64_t d2h = 0;
+  auto to_host = [&](uint32_t* dst, const uint32_t* src, size_t bytes) -> cudaError_t {
+    void* md = mapped_host(dst, bytes);
+    if (md) return pg::launch_copy16(md, src, bytes, h->num_sms, s);
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+  };
   if (graph && p->link_rounds > 0) {
-    PG_CUDA(cudaMemcpyAsync(graph, d_graph, n * p->degree * 4, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(to_host(graph, d_graph, n * p->degree * 4));
     d2h += n * p->degree * 4;
   }
   if (proj) {
-    PG_CUDA(cudaMemcpyAsync(proj, d_proj, n * p->proj_degree * 4, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(to_host(proj, d_proj, n * p->proj_degree * 4));
     d2h += n * p->proj_degree * 4;
   }
   PG_CUDA(cudaEventRecord(t3, s));

@@ -749,6 +749,35 @@ static cudaError_t launch_merge_e(const MergeArgs& a, int num_sms, cudaStream_t 
   return cudaGetLastError();
 }
 
+// 16-byte words from src to dst by the SMs (host memory mapped into the device address space
+// on one side): each thread moves four words per pass, so that every SM keeps many requests in
+// flight over the CPU-GPU link.
+__global__ void __launch_bounds__(256) k_copy16(uint4* __restrict__ dst,
+                                                const uint4* __restrict__ src, uint64_t words) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < words; i += 4 * stride) {
+    const uint4 v0 = src[i], v1 = src[i + stride], v2 = src[i + 2 * stride],
+                v3 = src[i + 3 * stride];
+    dst[i] = v0;
+    dst[i + stride] = v1;
+    dst[i + 2 * stride] = v2;
+    dst[i + 3 * stride] = v3;
+  }
+  for (; i < words; i += stride) dst[i] = src[i];
+}
+
+cudaError_t launch_copy16(void* dst, const void* src, uint64_t bytes, int num_sms,
+                          cudaStream_t st) {
+  if (bytes == 0) return cudaSuccess;
+  if ((bytes % 16) != 0 || (reinterpret_cast<uintptr_t>(dst) % 16) != 0 ||
+      (reinterpret_cast<uintptr_t>(src) % 16) != 0)
+    return cudaErrorInvalidValue;
+  k_copy16<<<static_cast<unsigned>(num_sms) * 4, 256, 0, st>>>(
+      static_cast<uint4*>(dst), static_cast<const uint4*>(src), bytes / 16);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_merge_prune(const MergeArgs& a, int num_sms, cudaStream_t st) {
   const uint32_t cmax = a.r + a.p;
   if (cmax <= 32) return launch_merge_e<1>(a, num_sms, st);

@@ -190,6 +190,10 @@ cudaError_t launch_reverse_lists(const uint32_t* offs, const uint32_t* edges, ui
                                  uint32_t r, uint32_t* rev, uint32_t* rev_num, int num_sms,
                                  cudaStream_t st);
 cudaError_t launch_merge_prune(const MergeArgs& a, int num_sms, cudaStream_t st);
+// bytes (a multiple of 16, both pointers 16-byte aligned) from src to dst by a kernel: used with
+// pinned host memory mapped into the device address space (cudaHostGetDevicePointer).
+cudaError_t launch_copy16(void* dst, const void* src, uint64_t bytes, int num_sms,
+                          cudaStream_t st);
 // Returns cudaErrorInvalidValue for parameter combinations the search kernel was not built for
 // (see search_supported).
 cudaError_t launch_search(const SearchArgs& a, int num_sms, size_t smem_optin, cudaStream_t st);

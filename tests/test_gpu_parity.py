@@ -218,6 +218,26 @@ def test_build_host_copy_split(pg, handle, n, d, seed):
     assert st.h2d_bytes == base.nbytes + gt.nbytes
 
 
+@pytest.mark.parametrize("n,d,seed", [(3001, 8, 23), (2999, 200, 24)])
+def test_build_host_pinned_buffers(pg, handle, n, d, seed):
+    """Pinned host buffers that the device can address are moved by the copy kernel (host to
+    device and back) instead of the copy engines; results equal the device-resident build."""
+    from paragraph_gb300 import datagen
+    base, gt = datagen.make_dataset(n, d, seed=seed)
+    params = pg.default_params(32, 64)
+    base_h = torch.from_numpy(base).pin_memory()
+    gt_h = torch.from_numpy(gt.view(np.int32)).pin_memory()
+    graph_h = torch.empty((n, params.degree), dtype=torch.int32).pin_memory()
+    proj_h = torch.empty((n, params.proj_degree), dtype=torch.int32).pin_memory()
+    st = handle.build_host_ptr(base_h.data_ptr(), n, d, gt_h.data_ptr(), gt.shape[0],
+                               graph_h.data_ptr(), proj_h.data_ptr(), params)
+    g_dev, p_dev, _, ref = _build_both(pg, handle, base, gt)
+    assert np.array_equal(graph_h.numpy().view(np.uint32), g_dev)
+    assert np.array_equal(proj_h.numpy().view(np.uint32), p_dev)
+    assert np.array_equal(g_dev, ref["graph"])
+    assert st.h2d_bytes == base.nbytes + gt.nbytes
+
+
 def test_builder_facade_and_savegraph(pg, golden_dir, tmp_path):
     f = load(golden_dir, "mix")
     b = pg.Builder(f["base"], f["gt"])
