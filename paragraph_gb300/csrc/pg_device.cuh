@@ -29,12 +29,33 @@ __device__ __forceinline__ void ld8(const float* p, float (&v)[8]) {
       : "l"(p));
 }
 
+// Rows of at least this many floats (1 KB) are read with 256-bit loads by the exact chains of the
+// plain prune and the merges when 32-byte aligned (their launchers pick the WIDE kernels): such
+// rows mostly come from DRAM, where half the load requests pay (measured at 1M x 512: merges
+// 251 -> 190 ms per build); the shorter rows of the L2-resident 1M x 200 workload were measured
+// faster with the float4 kernels.
+constexpr uint32_t kWideRowFloats = 256;
+
 // One FMA chain over d = 0..D-1: distance_between (Gbuilder.cuh:785-797), -(sum x[d]*y[d]).
-// Rows are 16-byte aligned when D % 4 == 0 (the library checks), so float4 loads keep the order.
+// Rows are 16-byte aligned when D % 4 == 0 (the library checks), so float4 loads keep the order;
+// with WIDE, 32-byte aligned rows (D % 8 == 0 on a 32-byte aligned base) take 256-bit loads, one
+// sector each, half the load requests of float4.
+template <bool WIDE = false>
 __device__ __forceinline__ float dist_seq(const float* __restrict__ x, const float* __restrict__ y,
                                           uint32_t d) {
   float s = 0.0f;
-  if ((d & 3u) == 0) {
+  if (WIDE && (d & 7u) == 0 &&
+      ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 31u) == 0) {
+    const uint32_t n8 = d >> 3;
+#pragma unroll 5
+    for (uint32_t i = 0; i < n8; i++) {
+      float u[8], v[8];
+      ld8(x + 8 * i, u);
+      ld8(y + 8 * i, v);
+#pragma unroll
+      for (int t = 0; t < 8; t++) s = fmaf(u[t], v[t], s);
+    }
+  } else if ((d & 3u) == 0) {
     const float4* a = reinterpret_cast<const float4*>(x);
     const float4* b = reinterpret_cast<const float4*>(y);
     const uint32_t n4 = d >> 2;

@@ -84,7 +84,7 @@ __global__ void k_validate_ids(const uint32_t* __restrict__ ids, uint64_t count,
 // ------------------------------------------------------------------ distances, E per lane
 // E independent FMA chains (one per candidate slot of this lane), interleaved for ILP.  Slots
 // with valid[s] == false are skipped and return FLT_MAX.
-template <int E>
+template <int E, bool WIDE>
 __device__ __forceinline__ void dist_seq_multi(const float* __restrict__ brow,
                                                const float* __restrict__ base, uint32_t d,
                                                const uint32_t (&id)[E], const bool (&valid)[E],
@@ -99,6 +99,25 @@ __device__ __forceinline__ void dist_seq_multi(const float* __restrict__ brow,
   }
   const float4* b4 = reinterpret_cast<const float4*>(brow);
   const uint32_t n4 = d >> 2;
+  if (WIDE && (d & 7u) == 0 &&
+      ((reinterpret_cast<uintptr_t>(base) | reinterpret_cast<uintptr_t>(brow)) & 31u) == 0) {
+    // 32-byte aligned rows: 256-bit loads, one sector each (half the requests of float4)
+#pragma unroll 2
+    for (uint32_t i = 0; i < (d >> 3); i++) {
+      float u[8];
+      ld8(brow + 8 * i, u);
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        float v[8];
+        ld8(reinterpret_cast<const float*>(rows[e]) + 8 * i, v);
+#pragma unroll
+        for (int t = 0; t < 8; t++) s[e] = fmaf(u[t], v[t], s[e]);
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < E; e++) out[e] = valid[e] ? -s[e] : FLT_MAX;
+    return;
+  }
   // four steps per pass keep (1 + E) * 4 row loads in flight: the rows come from L2, and the
   // chain's order leaves no other parallelism
 #pragma unroll 4
@@ -153,6 +172,7 @@ __device__ __forceinline__ bool occluded(const float* __restrict__ base, uint64_
 // (stop_at_tomb), or c.  Ids >= n count as occluded without a test.  win: 96 words per warp.
 constexpr uint32_t kWinNone = 0xFFFFFFFFu, kWinInvalid = 0xFFFFFFFEu;
 
+template <bool WIDE>
 __device__ uint32_t scan_kept(const float* __restrict__ base, uint64_t n, uint32_t d,
                               const uint32_t* ids_s, const float* dist_s, uint32_t j0, uint32_t c,
                               uint32_t* kept_s, uint32_t& K, uint32_t limit, bool stop_at_tomb,
@@ -190,7 +210,7 @@ __device__ uint32_t scan_kept(const float* __restrict__ base, uint64_t n, uint32
     bool o = false;
     if (my_w != kWinNone) {
       const uint32_t pos = wj[my_w];
-      o = dist_seq(base + static_cast<uint64_t>(ids_s[pos]) * d,
+      o = dist_seq<WIDE>(base + static_cast<uint64_t>(ids_s[pos]) * d,
                    base + static_cast<uint64_t>(kept_s[my_t]) * d, d) < dist_s[pos];
     }
     const unsigned mask = __ballot_sync(kFull, o);
@@ -260,7 +280,7 @@ __device__ __forceinline__ float key_dist(uint64_t key) {
 // ------------------------------------------------------------------ K2: prune + reverse
 // fusion_prune_reverse_kernel_v0 (Gbuilder.cuh:1093-1244).  PHASE1 reads the candidate row of
 // node b straight from the winner's ground truth (the K0 row) instead of a materialised graph.
-template <int E, bool PHASE1>
+template <int E, bool PHASE1, bool WIDE>
 __global__ void __launch_bounds__(256) k_prune_reverse(PruneArgs a) {
   constexpr int C_MAX = 32 * E;
   extern __shared__ uint32_t smem_u32[];
@@ -319,7 +339,7 @@ __global__ void __launch_bounds__(256) k_prune_reverse(PruneArgs a) {
       valid[s] = (x != kTomb && x != static_cast<uint32_t>(b) && x != kMaskedTomb);
     }
     float dist[E];
-    dist_seq_multi<E>(a.base + b * a.d, a.base, a.d, id, valid, dist);
+    dist_seq_multi<E, WIDE>(a.base + b * a.d, a.base, a.d, id, valid, dist);
     uint64_t key[E];
 #pragma unroll
     for (int s = 0; s < E; s++) {
@@ -348,7 +368,7 @@ __global__ void __launch_bounds__(256) k_prune_reverse(PruneArgs a) {
     __syncwarp();
     uint64_t checks = 0;
     uint32_t kc = 1;
-    uint32_t j = a.p > 1 ? scan_kept(a.base, a.n, a.d, ids_s, dist_s, 1, a.c, kept_s, kc, a.p, true,
+    uint32_t j = a.p > 1 ? scan_kept<WIDE>(a.base, a.n, a.d, ids_s, dist_s, 1, a.c, kept_s, kc, a.p, true,
                                      win_s, &checks)
                          : 1;
     uint32_t k = kc - 1;
@@ -537,7 +557,7 @@ __global__ void __launch_bounds__(256) k_reverse_lists(const uint32_t* __restric
 
 // One node's merged list (reverse entries, then pruned entries) with exact distances to the node,
 // sorted by (distance, position) into ids_s / dist_s[0 .. nn); E = slots per lane (nn <= 32 E).
-template <int E>
+template <int E, bool WIDE>
 __device__ __forceinline__ void merge_gather_sort(const MergeArgs& a, uint64_t b, uint32_t rn,
                                                   uint32_t nn, uint32_t* ids_s, float* dist_s) {
   const uint32_t lane = lane_id();
@@ -559,7 +579,7 @@ __device__ __forceinline__ void merge_gather_sort(const MergeArgs& a, uint64_t b
     valid[s] = j < nn && x != kTomb;
   }
   float dist[E];
-  dist_seq_multi<E>(a.base + b * a.d, a.base, a.d, id, valid, dist);
+  dist_seq_multi<E, WIDE>(a.base + b * a.d, a.base, a.d, id, valid, dist);
   uint64_t key[E];
 #pragma unroll
   for (int s = 0; s < E; s++) {
@@ -581,7 +601,7 @@ __device__ __forceinline__ void merge_gather_sort(const MergeArgs& a, uint64_t b
 // fusion_merge_sort_prune_kernel (Gbuilder.cuh:1467-1601): merged list = reverse entries then
 // pruned entries (pr_sort_list view); sort by distance keeping that order on ties; RNG prune
 // into the out row; non-strict fill with first-occurrence marking; tomb padding.
-template <int E>
+template <int E, bool WIDE>
 __global__ void __launch_bounds__(256) k_merge_prune(MergeArgs a) {
   constexpr int C_MAX = 32 * E;
   extern __shared__ uint32_t smem_u32[];
@@ -607,18 +627,19 @@ __global__ void __launch_bounds__(256) k_merge_prune(MergeArgs a) {
     if (lane == 0) ev += nn;
     // the merged lists are mostly short: size the distance slots and the sort to this one
     if (nn <= 32)
-      merge_gather_sort<1>(a, b, rn, nn, ids_s, dist_s);
+      merge_gather_sort<1, WIDE>(a, b, rn, nn, ids_s, dist_s);
     else if (E >= 2 && nn <= 64)
-      merge_gather_sort<(E >= 2 ? 2 : 1)>(a, b, rn, nn, ids_s, dist_s);
+      merge_gather_sort<(E >= 2 ? 2 : 1), WIDE>(a, b, rn, nn, ids_s, dist_s);
     else
-      merge_gather_sort<E>(a, b, rn, nn, ids_s, dist_s);
+      merge_gather_sort<E, WIDE>(a, b, rn, nn, ids_s, dist_s);
     __syncwarp();
     if (lane == 0) out_s[0] = ids_s[0];
     __syncwarp();
     uint64_t checks = 0;
     uint32_t kc = 1;
     if (a.degree > 1)
-      scan_kept(a.base, a.n, a.d, ids_s, dist_s, 1, nn, out_s, kc, a.degree, false, win_s, &checks);
+      scan_kept<WIDE>(a.base, a.n, a.d, ids_s, dist_s, 1, nn, out_s, kc, a.degree, false, win_s,
+                      &checks);
     uint32_t k = kc - 1;
     if (!a.strict && k < a.degree - 1) {
       for (uint32_t i = lane; i < nn; i += 32) added_s[i] = 0;
@@ -701,11 +722,20 @@ cudaError_t launch_validate_ids(const uint32_t* ids, uint64_t count, uint64_t n,
   return cudaGetLastError();
 }
 
+// The 256-bit-load kernels for rows of kWideRowFloats or more on a 32-byte aligned base.
+static bool wide_rows(const float* base, uint32_t d) {
+  return d >= kWideRowFloats && (d % 8) == 0 && (reinterpret_cast<uintptr_t>(base) % 32) == 0;
+}
+
 template <int E, bool P1>
 static cudaError_t launch_prune_e(const PruneArgs& a, int num_sms, cudaStream_t st) {
   const int threads = 256;
   const size_t smem = (threads / 32) * (3 * 32 * E + 96) * sizeof(uint32_t);
-  k_prune_reverse<E, P1><<<grid_for(a.n, threads / 32, num_sms, 8), threads, smem, st>>>(a);
+  const unsigned grid = grid_for(a.n, threads / 32, num_sms, 8);
+  if (wide_rows(a.base, a.d))
+    k_prune_reverse<E, P1, true><<<grid, threads, smem, st>>>(a);
+  else
+    k_prune_reverse<E, P1, false><<<grid, threads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -745,7 +775,11 @@ template <int E>
 static cudaError_t launch_merge_e(const MergeArgs& a, int num_sms, cudaStream_t st) {
   const int threads = 256;
   const size_t smem = (threads / 32) * (3 * 32 * E + 8 * E + 96) * sizeof(uint32_t);
-  k_merge_prune<E><<<grid_for(a.n, threads / 32, num_sms, 8), threads, smem, st>>>(a);
+  const unsigned grid = grid_for(a.n, threads / 32, num_sms, 8);
+  if (wide_rows(a.base, a.d))
+    k_merge_prune<E, true><<<grid, threads, smem, st>>>(a);
+  else
+    k_merge_prune<E, false><<<grid, threads, smem, st>>>(a);
   return cudaGetLastError();
 }
 

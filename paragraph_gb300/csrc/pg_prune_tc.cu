@@ -390,8 +390,9 @@ __global__ void __launch_bounds__(kTile, S == 2 ? 4 : 3) k_prune_tc(const PruneA
                               c_seq * np2 * nr + fabsf(dhat) * 9.5367431640625e-07f + 1e-30f;
           bool yes = dhat + bound < dist;
           if (!yes && !(dhat - bound >= dist)) {  // inside the margin (or NaN): exact chain
-            yes = dist_seq(a.base + static_cast<uint64_t>(x) * d,
-                           a.base + static_cast<uint64_t>(ri) * d, d) < dist;
+            // a re-score holds up the node's scan: 256-bit loads whatever the row length
+            yes = dist_seq<true>(a.base + static_cast<uint64_t>(x) * d,
+                                 a.base + static_cast<uint64_t>(ri) * d, d) < dist;
             nres++;
           }
           if (yes) fo = t_k;
