@@ -292,8 +292,11 @@ def test_screened_build_matches_plain_and_oracle_fixture(pg, handle, golden_dir,
 
 
 @pytest.mark.parametrize("screen", [1, 3])  # BF16, FP16
-@pytest.mark.parametrize("n,d,seed", [(20000, 200, 1), (6000, 64, 7), (3000, 8, 8)])
+@pytest.mark.parametrize("n,d,seed", [(20000, 200, 1), (6000, 64, 7), (3000, 8, 8),
+                                      (4999, 100, 9)])
 def test_screened_build_matches_oracle(pg, handle, n, d, seed, screen):
+    """(4999, 100): an odd node count leaves the last two-node tile of the tensor-core prune half
+    empty, and D = 100 ends in a chunk of 4 columns (one K = 16 MMA step on zero padding)."""
     from paragraph_gb300 import datagen
     base, gt = datagen.make_dataset(n, d, seed=seed)
     g, p, st, ref = _build_both(pg, handle, base, gt, screen=screen)
