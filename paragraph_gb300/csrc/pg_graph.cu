@@ -136,29 +136,6 @@ __device__ __forceinline__ void dist_seq_multi(const float* __restrict__ brow,
   for (int e = 0; e < E; e++) out[e] = valid[e] ? -s[e] : FLT_MAX;
 }
 
-// Occlusion test of candidate p (distance dp to the node) against kept[0..k] in order
-// (Gbuilder.cuh:1163-1181): true if some kept r has dist(p, r) < dp.  Lanes test 32 kept entries
-// at a time; *checks gets the number of comparisons the reference makes (up to the first hit).
-__device__ __forceinline__ bool occluded(const float* __restrict__ base, uint64_t n, uint32_t d,
-                                         uint32_t p, float dp, const uint32_t* kept, uint32_t k,
-                                         uint64_t* checks) {
-  const uint32_t lane = lane_id();
-  if (p >= n) return true;  // only reachable after an input error was flagged
-  const float* prow = base + static_cast<uint64_t>(p) * d;
-  for (uint32_t t0 = 0; t0 <= k; t0 += 32) {
-    const uint32_t t = t0 + lane;
-    bool o = false;
-    if (t <= k && kept[t] < n) o = dist_seq(prow, base + static_cast<uint64_t>(kept[t]) * d, d) < dp;
-    const unsigned m = __ballot_sync(kFull, o);
-    if (m) {
-      *checks += static_cast<uint32_t>(__ffs(static_cast<int>(m)));
-      return true;
-    }
-    *checks += min(32u, k + 1 - t0);
-  }
-  return false;
-}
-
 // The occlusion scan of fusion_prune_reverse_kernel_v0 (Gbuilder.cuh:1150-1199) and
 // fusion_merge_sort_prune_kernel over the sorted candidates ids_s/dist_s[j0 .. c): in order, a
 // candidate is kept when no kept entry lies closer to it than the node does (exact FP32 chain),
@@ -166,8 +143,9 @@ __device__ __forceinline__ bool occluded(const float* __restrict__ base, uint64_
 // entry) pairs of a window of consecutive undecided candidates, each candidate against the kept
 // entries it has not been tested against yet.  Candidates are decided from the front of the
 // window -- occluded ones dropped, the first unoccluded one kept, which sends the later ones back
-// for one more test against it.  Kept entries and the evaluation count (tests up to the first
-// occluder, as occluded() counts them) equal the one-candidate-at-a-time scan.  kept_s[0 .. K)
+// for one more test against it.  Kept entries and the evaluation count (the reference's count of
+// tests: up to and including the first occluder, in kept order) equal the one-candidate-at-a-time
+// scan (Gbuilder.cuh:1163-1181).  kept_s[0 .. K)
 // on entry; returns where that scan stops: the candidate that filled the list, the first tomb
 // (stop_at_tomb), or c.  Ids >= n count as occluded without a test.  win: 96 words per warp.
 constexpr uint32_t kWinNone = 0xFFFFFFFFu, kWinInvalid = 0xFFFFFFFEu;
