@@ -471,7 +471,7 @@ def run_ours(args):
     # K0, K2 + CSR (5), K3 = 8; per link round search, prune + CSR (5), merge = 8; once per build
     # the seed-distance pass and, when screened, the norm pre-pass
     once = (1 if params.link_rounds > 0 else 0) + (
-        1 if (screen and params.link_rounds > 0 and args.beam <= 96) else 0)
+        1 if (screen and params.link_rounds > 0 and args.beam <= 128) else 0)
     launches_per_build = 8 + 8 * params.link_rounds + once
     tuning = None
     if args.autotune:
@@ -787,7 +787,7 @@ def run_batched(args):
     with ClockSampler(0) as clocks:
         res, st, ms = batched_measure(h, stream, base, gt, node_off, sizes, args.degree,
                                       args.beam, screen, args.steps, args.warmup)
-    launches = (10 + 8 * 2 + 1 + (1 if screen and args.beam <= 96 else 0)) * args.steps
+    launches = (10 + 8 * 2 + 1 + (1 if screen and args.beam <= 128 else 0)) * args.steps
     line = {"metric": metric_name(args, total), "value": st.evals_total / (ms / 1e3),
             "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
