@@ -308,8 +308,9 @@ def test_screened_build_matches_oracle(pg, handle, n, d, seed, screen):
     assert sum(st.rescored) < 0.5 * sum(st.evals_prune)
 
 
+@pytest.mark.parametrize("beam", [64, 128])  # two nodes per tensor-core tile, one
 @pytest.mark.parametrize("screen", [1, 3])  # BF16, FP16
-def test_screened_build_extreme_scales(pg, handle, screen):
+def test_screened_build_extreme_scales(pg, handle, screen, beam):
     """Points scaled by 1e-6 .. 1e5: FP16 copies with subnormal coordinates (the norm bounds carry
     their norm, in case the tensor core flushes them) and coordinates beyond FP16's range (infinite
     norm bounds: every test of such a point goes to the exact chain).  Edges still equal the
@@ -319,7 +320,7 @@ def test_screened_build_extreme_scales(pg, handle, screen):
     f = 10.0 ** np.random.default_rng(9).uniform(-6, 5, base.shape[0])
     base = np.ascontiguousarray(base * f[:, None].astype(np.float32), dtype=np.float32)
     assert np.isfinite(base).all() and (np.abs(base) > 65504).any()
-    g, p, st, ref = _build_both(pg, handle, base, gt, screen=screen)
+    g, p, st, ref = _build_both(pg, handle, base, gt, beam=beam, screen=screen)
     assert np.array_equal(p, ref["proj"])
     bad = (g != ref["graph"]).any(axis=1)
     assert not bad.any(), f"{bad.sum()} rows differ"
@@ -354,10 +355,11 @@ def test_screened_build_wide_beams(pg, handle, n, d, degree, seed, cosine, beam,
     assert sum(st.rescored) < 0.5 * sum(st.evals_prune)
 
 
+@pytest.mark.parametrize("beam", [96, 128])
 @pytest.mark.parametrize("screen", [1, 3])
-def test_screened_96_with_hubs_and_duplicates(pg, handle, golden_dir, screen):
+def test_screened_wide_beams_with_hubs_and_duplicates(pg, handle, golden_dir, screen, beam):
     f = load(golden_dir, "edge")
-    g, p, st, ref = _build_both(pg, handle, f["base"], f["gt"], degree=32, beam=96,
+    g, p, st, ref = _build_both(pg, handle, f["base"], f["gt"], degree=32, beam=beam,
                                 screen=screen)
     assert np.array_equal(g, ref["graph"])
     assert st.evals_total == ref["stats"]["evals_total"]
