@@ -15,7 +15,7 @@ and graph + projection device->host inside the timed region.
 
 --impl reference times the CPU restatement of the path (the oracle; the reference's own code for
 this path is GPU-only and its CPU RoarGraph path does not build on this Arm host) on all host
-cores, on a bounded sample of the same workload.
+cores: one whole build of the same workload per step.
 """
 from __future__ import annotations
 
