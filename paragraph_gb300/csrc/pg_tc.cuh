@@ -1,7 +1,7 @@
 // pg_tc.cuh -- sm_103a building blocks shared by the tensor-core kernels: mbarriers with bounded
-// waits, TMA tile and row-gather loads, tcgen05 MMA issue / commit / TMEM loads, shared-memory
-// matrix descriptors, and the tensor-map encoder (reached through the runtime's driver entry
-// points, so the library does not link the driver library).
+// waits, TMA tile loads, tcgen05 MMA issue / commit / TMEM loads, shared-memory matrix
+// descriptors, and the tensor-map encoder (reached through the runtime's driver entry points, so
+// the library does not link the driver library).
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -76,19 +76,6 @@ __device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, uint
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(saddr(bar))
       : "memory");
 }
-// Four rows y0..y3 of a 2-D tensor map whose box is one row high, columns x .. x + box - 1
-// each, into four consecutive box-sized rows at dst.
-__device__ __forceinline__ void tma_gather4(void* dst, const CUtensorMap* map, uint32_t x,
-                                            uint32_t y0, uint32_t y1, uint32_t y2, uint32_t y3,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(saddr(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y0), "r"(y1), "r"(y2), "r"(y3),
-      "r"(saddr(bar))
-      : "memory");
-}
-
 // ---- shared-memory matrix descriptors (K-major operands), descriptor version 1 (bits 46-47)
 // Tile written by TMA with 128-byte swizzling: rows of 128 bytes in 8-row atoms of 1024 bytes
 // (stride byte offset), one atom along K (leading byte offset unused), swizzle mode 2 (bits
