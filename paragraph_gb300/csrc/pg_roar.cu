@@ -36,65 +36,17 @@ struct RoarSmem {
   uint32_t fin[kRoarCap + kRoarRes];
 };
 
-// compare() (tests/test_t2iend.cu:31-80), negated inner product in its exact FP32 order.  Rows
-// are 16-byte aligned (d % 4 == 0).
-__device__ __forceinline__ float dist_avx(const float* __restrict__ a, const float* __restrict__ b,
-                                          uint32_t d) {
-  const float4* a4 = reinterpret_cast<const float4*>(a);
-  const float4* b4 = reinterpret_cast<const float4*>(b);
-  float s[16];
-#pragma unroll
-  for (int l = 0; l < 16; l++) s[l] = 0.0f;
-  uint32_t i = 0;
-  for (; i + 16 <= d; i += 16) {
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-      const float4 x = __ldg(a4 + (i >> 2) + c);
-      const float4 y = __ldg(b4 + (i >> 2) + c);
-      s[4 * c + 0] = fmaf(x.x, y.x, s[4 * c + 0]);
-      s[4 * c + 1] = fmaf(x.y, y.y, s[4 * c + 1]);
-      s[4 * c + 2] = fmaf(x.z, y.z, s[4 * c + 2]);
-      s[4 * c + 3] = fmaf(x.w, y.w, s[4 * c + 3]);
-    }
-  }
-  float s8[8];
-#pragma unroll
-  for (int l = 0; l < 8; l++) s8[l] = s[8 + l] + s[l];
-  if (d - i >= 8) {
-#pragma unroll
-    for (int c = 0; c < 2; c++) {
-      const float4 x = __ldg(a4 + (i >> 2) + c);
-      const float4 y = __ldg(b4 + (i >> 2) + c);
-      s8[4 * c + 0] = fmaf(x.x, y.x, s8[4 * c + 0]);
-      s8[4 * c + 1] = fmaf(x.y, y.y, s8[4 * c + 1]);
-      s8[4 * c + 2] = fmaf(x.z, y.z, s8[4 * c + 2]);
-      s8[4 * c + 3] = fmaf(x.w, y.w, s8[4 * c + 3]);
-    }
-    i += 8;
-  }
-  float s4[4];
-#pragma unroll
-  for (int l = 0; l < 4; l++) s4[l] = s8[4 + l] + s8[l];
-  if (d - i >= 4) {
-    const float4 x = __ldg(a4 + (i >> 2));
-    const float4 y = __ldg(b4 + (i >> 2));
-    s4[0] = fmaf(x.x, y.x, s4[0]);
-    s4[1] = fmaf(x.y, y.y, s4[1]);
-    s4[2] = fmaf(x.z, y.z, s4[2]);
-    s4[3] = fmaf(x.w, y.w, s4[3]);
-  }
-  return -((s4[0] + s4[1]) + (s4[2] + s4[3]));
-}
-
 __device__ __forceinline__ const float* row_of(const float* base, uint32_t d, uint32_t id) {
   return base + static_cast<uint64_t>(id) * d;
 }
 
-// compare() computed by a group of 8 lanes: lane l of the group holds the accumulators of
-// elements 16c + l and 16c + 8 + l, so the 8+8 fold happens in the lane, the 4+4 fold and the two
-// horizontal adds by shuffles inside the group.  Every lane of the warp calls it (the shuffles
-// are warp-wide); the distance is valid in lane 0 of each group.  Same FP32 operations, in the
-// same order, as dist_avx; the group's loads are contiguous.
+// compare() (tests/test_t2iend.cu:31-80), the negated inner product in its exact FP32 order --
+// 16 accumulators over 16-wide chunks, folded 8+8, an 8-wide FMA step, folded 4+4, a 4-wide
+// step, then ((s0 + s1) + (s2 + s3)) -- computed by a group of 8 lanes: lane l of the group holds
+// the accumulators of elements 16c + l and 16c + 8 + l, so the 8+8 fold happens in the lane, the
+// 4+4 fold and the two horizontal adds by shuffles inside the group.  Every lane of the warp
+// calls it (the shuffles are warp-wide); the distance is valid in lane 0 of each group; the
+// group's loads are contiguous.
 __device__ __forceinline__ float dist_avx8(const float* __restrict__ a,
                                            const float* __restrict__ b, uint32_t d, uint32_t l8) {
   float lo = 0.0f, hi = 0.0f;
